@@ -1,0 +1,316 @@
+"""Benchmark: exact Apriori mining of the dense K=2 stress workload on one GB300.
+
+Workload (default ``dense_k2``): 2,000,000 transactions x 4,096 items, item
+i present independently with probability p_i ~ Beta(2, 30) (hash-defined
+bits, generated on the device), min_support 0.002, max_length 3. One step is
+one complete ``mine()`` of that workload: K=1, the ~8.4M pair candidates and
+the ~4.4e9 triple candidates, every survivor compacted into lexsorted
+levels. The bitvectors (1.02 GB) are larger than L2, so no flush is needed
+between steps.
+
+Prints ONE JSON line (rank 0):
+  value         seconds per mine, batched form (device-resident input)
+  plain         the one-launch-per-prefix-group form on the same input
+  e2e           seconds per mine through apriori(bitvecs=...) with the
+                bitvectors copied from pinned host memory and the itemsets
+                copied back inside the timed region
+  roofline      the dominant counting kernel: algorithmic bytes per launch over
+                its CUDA-event time, against the measured HBM copy peak
+  cpu_baseline  the CPU oracle on a bounded sample, extrapolated per row
+``--impl reference`` times the CPU restatement of the reference's counting
+path (the oracle) on the host cores instead, on the same workload.
+
+Multi-GPU: the path does not shard in this engine (replicas only); under
+torchrun every rank mines its own copy and the max over ranks is reported.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    "dense_k2": dict(n_items=4096, n_rows=2_000_000, min_support=0.002, max_length=3, seed=0, hash_seed=12345),
+    "dense_k2_small": dict(n_items=1024, n_rows=500_000, min_support=0.002, max_length=3, seed=0, hash_seed=12345),
+}
+
+
+def _peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.proc = None
+        self.device_index = device_index
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(device_index), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dense_k2_device(pkg, lib, spec):
+    import torch
+
+    syn = pkg.synthetic
+    p = syn.dense_k2_probs(spec["n_items"], seed=spec["seed"])
+    thr = torch.from_numpy(syn.bernoulli_thresholds(p).view(np.int64)).cuda()
+    n_rows = spec["n_rows"]
+    ld = (n_rows + 63) // 64
+    bv = torch.empty((spec["n_items"], ld), dtype=torch.int64, device="cuda")
+    st = lib.etm_synth_bernoulli(thr.data_ptr(), spec["n_items"], n_rows, spec["hash_seed"], bv.data_ptr(), ld,
+                                 torch.cuda.current_stream().cuda_stream)
+    if st != 0:
+        raise RuntimeError(lib.etm_last_error().decode())
+    torch.cuda.synchronize()
+    return bv.view(torch.uint64)
+
+
+def cpu_sample(pkg, spec, budget_s: float = 20.0) -> dict:
+    """The CPU oracle on a bounded slice of the workload (same items and thresholds, fewer rows),
+    extrapolated linearly in rows to the full workload."""
+    from oracle import miner
+
+    syn = pkg.synthetic
+    p = syn.dense_k2_probs(spec["n_items"], seed=spec["seed"])
+    thr = syn.bernoulli_thresholds(p)
+    rows = 2048
+    best = None
+    while True:
+        bv = syn.bernoulli_bitvecs(thr, rows, spec["hash_seed"])
+        t0 = time.perf_counter()
+        miner.mine_bitvecs(bv, rows, spec["min_support"], spec["max_length"])
+        dt = time.perf_counter() - t0
+        best = (rows, dt)
+        if dt > budget_s / 4 or rows >= spec["n_rows"]:
+            break
+        rows = min(spec["n_rows"], rows * 4)
+    rows, dt = best
+    scale = spec["n_rows"] / rows
+    return {"value": dt * scale, "unit": "s", "cores": 1, "kind": "port",
+            "sample": f"oracle/miner.py mine_bitvecs on the first {rows:,} of {spec['n_rows']:,} rows "
+                      f"(same items and thresholds, min_support {spec['min_support']}), {dt:.2f} s, "
+                      f"extrapolated x{scale:.0f} in rows"}
+
+
+def run_reference(args, spec) -> None:
+    pkg = _pkg()
+    base = cpu_sample(pkg, spec, budget_s=max(5.0, 20.0 / max(1, args.steps)))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": base["value"], "unit": "s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["value"] * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": args.workload, **spec},
+        "cpu_baseline": base,
+        "e2e": {"value": base["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _pkg():
+    import __graft_entry__ as g
+
+    return g.package()
+
+
+METRIC = "mine() seconds, dense K=2 stress (2M x 4096, s=0.002, max_length=3), exact counts, batched form"
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--workload", default="dense_k2", choices=sorted(WORKLOADS))
+    ap.add_argument("--method", default=None, choices=["popcount", "tensor"])
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparator")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    spec = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, spec)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    pkg = _pkg()
+    pkg.build_library()
+    lib = pkg.load_library()
+    from importlib import import_module
+
+    engm = import_module(pkg.__name__ + ".engine")
+    method = args.method or engm.DEFAULT_METHOD
+    bv = dense_k2_device(pkg, lib, spec)
+    n_rows = spec["n_rows"]
+    eng = engm.Engine(form="batched", method=method)
+    eng.profile_kernels = True
+
+    def one(e):
+        return e.mine(bv, n_rows, spec["min_support"], spec["max_length"])
+
+    for _ in range(args.warmup):
+        out = one(eng)
+    torch.cuda.synchronize()
+    ref_sizes = [s.n_frequent for s in out.stats]
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    eng.reset_kernel_times()
+    launches0 = eng.launches
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(args.steps):
+        out = one(eng)
+        assert [s.n_frequent for s in out.stats] == ref_sizes
+    end.record()
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = start.elapsed_time(end) / args.steps
+    launches = (eng.launches - launches0) // args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    kern = eng.kernel_report()
+
+    # Plain form (one counting launch per prefix group): the comparator.
+    plain = None
+    if not args.no_plain:
+        pe = engm.Engine(form="plain", method=method)
+        one(pe)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        po = one(pe)
+        torch.cuda.synchronize()
+        plain_s = time.perf_counter() - t0
+        assert [s.n_frequent for s in po.stats] == ref_sizes
+        plain = {"value": plain_s, "unit": "s", "speedup_batched": plain_s / (ms / 1e3)}
+
+    # End to end through the public API: pinned host bitvectors in, itemsets out.
+    host = torch.empty(bv.shape, dtype=torch.int64, pin_memory=True)
+    host.copy_(bv.view(torch.int64))
+    col_to_item = {c: c for c in range(spec["n_items"])}
+    dev = torch.empty_like(bv.view(torch.int64))
+    e2e_ms = []
+    d2h = 0
+    for i in range(args.steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev.copy_(host, non_blocking=True)
+        df = pkg.apriori(bitvecs=(dev.view(torch.uint64), col_to_item, n_rows), min_support=spec["min_support"],
+                         max_length=spec["max_length"], engine=eng, warn_complexity=False)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) * 1e3
+        if i > 0:
+            e2e_ms.append(dt)
+        n_items_out = len(df)
+    d2h = sum(int(np.prod(lv.rows.shape)) * 4 + lv.n * 4 for lv in out.levels) + len(out.level1_cols) * 12
+    h2d = int(host.numel() * 8)
+
+    peaks = _peaks()
+    roof = None
+    if kern:
+        top = max(kern.values(), key=lambda r: r["ms"])
+        achieved = top["bytes"] / (top["ms"] / top["launches"] / 1e3) / top["launches"] / 1e9 if top["ms"] > 0 else 0.0
+        roof = {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                "traffic": None, "launches_per_step": top["launches"] / args.steps,
+                "ms_per_step": top["ms"] / args.steps, "share_of_step": (top["ms"] / args.steps) / ms}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_sample(pkg, spec)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic (hash-defined Bernoulli bits, on device)",
+            "config": {"workload": args.workload, **spec, "method": method, "form": "batched",
+                       "l2": "inputs (1.02 GB of bitvectors) larger than L2; no flush",
+                       "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "levels": [{"k": s.k, "candidates": s.n_candidates, "frequent": s.n_frequent, "ms": round(s.ms, 2)}
+                       for s in out.stats],
+            "plain": plain,
+            "e2e": {"value": statistics.median(e2e_ms) / 1e3, "unit": "s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "itemsets": n_items_out},
+            "roofline": roof,
+            "kernels": kern,
+            "cpu_baseline": cpu,
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -19,18 +19,18 @@ from ._lib import build_library, lib_path, load_library
 __all__ = ["synthetic", "build_library", "load_library", "lib_path"]
 
 
+_LAZY = {
+    "apriori": "api", "result_pairs": "api", "ProfilingSession": "api", "ItemsetFrame": "api",
+    "mine": "engine", "MineOutput": "engine", "Engine": "engine",
+    "Server": "serve",
+}
+
+
 def __getattr__(name):
     # The driver modules import torch; load them on first use.
-    if name in ("apriori", "result_pairs", "ProfilingSession"):
-        from . import apriori as _a
+    mod = _LAZY.get(name)
+    if mod is None:
+        raise AttributeError(name)
+    import importlib
 
-        return getattr(_a, name)
-    if name in ("mine", "MineOutput", "Engine"):
-        from . import engine as _e
-
-        return getattr(_e, name)
-    if name in ("Server",):
-        from . import serve as _s
-
-        return getattr(_s, name)
-    raise AttributeError(name)
+    return getattr(importlib.import_module(f"{__name__}.{mod}"), name)

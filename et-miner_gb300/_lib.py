@@ -69,7 +69,7 @@ def build_library(verbose: bool = False, force: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as pool:
         objs = list(pool.map(compile_one, srcs))
     tmp = out.with_suffix(".so.tmp")
-    cmd = [_nvcc(), f"-gencode=arch=compute_{ARCH},code=sm_{ARCH}", "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lcuda"]
+    cmd = [_nvcc(), f"-gencode=arch=compute_{ARCH},code=sm_{ARCH}", "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
@@ -88,17 +88,17 @@ SIGNATURES: dict[str, tuple] = {
     "etm_version": (ctypes.c_int, []),
     "etm_last_error": (ctypes.c_char_p, []),
     "etm_device_sm_count": (ctypes.c_int, []),
-    "etm_build_bitvecs": (ctypes.c_int, [_P, _P, _P, _I64, _I64, _I64, _I64, _P, _P]),
+    "etm_build_bitvecs": (ctypes.c_int, [_P, _P, _I64, _P, _I64, _I64, _I64, _I64, _P, _P]),
     "etm_popcount_cols": (ctypes.c_int, [_P, _I64, _I64, _I64, _P, _P]),
     "etm_gather_cols": (ctypes.c_int, [_P, _I64, _P, _I32, _I64, _P, _I64, _P]),
     "etm_synth_bernoulli": (ctypes.c_int, [_P, _I32, _I64, _U64, _P, _I64, _P]),
-    "etm_pair_counts": (ctypes.c_int, [_P, _I64, _I32, _I64, _I32, _P, _P]),
-    "etm_gram_workspace_bytes": (ctypes.c_int, [_I32, _I64, _P]),
-    "etm_level_groups": (ctypes.c_int, [_P, _I64, _I32, _P, _P, _P, _P, _P]),
-    "etm_level_project": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _I64, _I64, _I64, _P, _P, _I64, _P, _P]),
-    "etm_level_count": (ctypes.c_int, [_P, _I64, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P, _P, _I64, _I32, _I32, _I32, _P, _P]),
-    "etm_level_compact": (ctypes.c_int, [_P, _I64, _P, _P, _I64, _I64, _P, _I32, _I32, _P, _P, _P, _P, _I64, _P, _P]),
-    "etm_k2_compact": (ctypes.c_int, [_P, _P, _I32, _I32, _P, _I32, _P, _P, _P, _P, _I64, _P, _P]),
+    "etm_level_groups": (ctypes.c_int, [_P, _I64, _I32, _P, _P, _P, _P, _P, _I64, _P]),
+    "etm_classify": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _P, _P, _I64, _I64, _I32, _P, _P, _P]),
+    "etm_count_tiles": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P]),
+    "etm_count_cands": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _P, _P]),
+    "etm_level_compact": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _P, _P, _P, _I64, _I64, _I32, _P, _P, _I64, _P, _P, _I64, _P]),
+    "etm_level_subsets": (ctypes.c_int, [_P, _P, _I64, _I32, _P, _P, _I64, _P, _P, _P]),
+    "etm_select_rows": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I32, _P, _P, _P, _P, _I64, _P, _P, _I64, _P]),
 }
 
 

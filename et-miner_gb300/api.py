@@ -1,0 +1,462 @@
+"""``apriori()``: the drop-in for ET-Miner's GPU route (core/apriori.py:303-754).
+
+Same signature, parameter validation and error types as the reference's
+``apriori``. Two inputs reach the GB300 engine:
+
+* ``bitvecs=(array, col_to_item, n_transactions)``: the caller's
+  C-contiguous uint64 device array ``(n_cols, ceil(N/64))`` (any object with
+  ``__cuda_array_interface__``, or a torch CUDA tensor), read only
+  (core/apriori.py:477-548);
+* ``transactions`` with ``use_gpu=True``: a list column (polars DataFrame or
+  LazyFrame when polars is installed, a pyarrow Table, a dict of lists, or a
+  plain list of item lists). The items are deduplicated per row and counted
+  on the host, the frequent ones coded to columns, and the column bitvectors
+  are built on the device by ``etm_build_bitvecs`` (the reference's input
+  layer, gpu/input_layer.py:469-544 and gpu/csr_bitvec.py:63-155).
+
+The routes this engine does not implement (the CPU route, SON streaming,
+several GPUs, the per-level parquet flush, resume, anchors) raise
+``ValueError`` naming the option, rather than silently answering another
+question (the reference's own rule, core/apriori.py:109-251).
+
+The result is a polars DataFrame when polars is importable, else a pyarrow
+Table, with columns ``itemset`` (list of ascending item ids: Int64, or the
+input's UInt64 / wide dtype kept, core/result.py:30-54) and ``support``
+(Float64 = count / N). Row order is not part of the contract.
+"""
+
+from __future__ import annotations
+
+import math
+import numbers
+import time
+import warnings
+from dataclasses import dataclass, field
+from math import comb
+from typing import Any
+
+import numpy as np
+
+from .engine import Engine, MineOutput, min_count
+
+try:  # optional: results come back as polars frames when it is installed
+    import polars as _pl
+except Exception:  # pragma: no cover - polars is absent in the build image
+    _pl = None
+
+try:  # optional: pyarrow tables in and out when it is installed
+    import pyarrow as pa
+except Exception:  # pragma: no cover - the GPU machine has no pyarrow
+    pa = None
+
+
+@dataclass
+class Phase:
+    name: str
+    ms: float
+    extra: dict = field(default_factory=dict)
+
+
+class ProfilingSession:
+    """Per-phase wall times of one mining call (the reference's core/profiling.py:26-177, in brief).
+
+    ``phases`` holds one entry per level (``k1``, ``k2``, ...) with the
+    candidates, frequent itemsets, prefix groups and launches of the level.
+    """
+
+    def __init__(self) -> None:
+        self.phases: list[Phase] = []
+        self._open: tuple[str, float] | None = None
+
+    def start_phase(self, name: str) -> None:
+        self._open = (name, time.perf_counter())
+
+    def end_phase(self, **extra) -> None:
+        if self._open is not None:
+            name, t0 = self._open
+            self.phases.append(Phase(name, (time.perf_counter() - t0) * 1e3, dict(extra)))
+            self._open = None
+
+    def record_phase(self, name: str, ms: float, **extra) -> None:
+        self.phases.append(Phase(name, ms, dict(extra)))
+
+    @property
+    def total_ms(self) -> float:
+        return sum(p.ms for p in self.phases)
+
+    def summary(self) -> str:
+        return "\n".join(f"{p.name:>6s} {p.ms:10.2f} ms {p.extra}" for p in self.phases)
+
+
+def _warn_complexity(n_frequent_items: int, min_support: float) -> None:
+    """Warn when the pair count is large (core/apriori.py:38-61)."""
+    n_pairs = comb(n_frequent_items, 2) if n_frequent_items > 1 else 0
+    if n_pairs > 10_000_000:
+        warnings.warn(f"Very large computation ahead: {n_frequent_items:,} frequent items, {n_pairs:,} candidate "
+                      f"pairs (min_support={min_support})", UserWarning, stacklevel=3)
+    elif n_pairs > 1_000_000:
+        warnings.warn(f"Large computation: {n_pairs:,} candidate pairs.", UserWarning, stacklevel=3)
+
+
+def _validate_parameters(min_support, max_length, batch_size, sparse_from_k=None, prune_apriori=True) -> None:
+    """Parameter checks of core/apriori.py:64-106."""
+    if isinstance(min_support, bool) or not isinstance(min_support, (int, float)):
+        raise TypeError(f"min_support must be numeric, got {type(min_support).__name__}")
+    if not 0.0 <= min_support <= 1.0:
+        raise ValueError(f"min_support must be in range [0.0, 1.0], got {min_support}")
+    if max_length is not None:
+        if isinstance(max_length, bool) or not isinstance(max_length, int):
+            raise TypeError(f"max_length must be int or None, got {type(max_length).__name__}")
+        if max_length < 1:
+            raise ValueError(f"max_length must be >= 1, got {max_length}")
+    if batch_size is not None:
+        if isinstance(batch_size, bool) or not isinstance(batch_size, int):
+            raise TypeError(f"batch_size must be int or None, got {type(batch_size).__name__}")
+        if batch_size < 1:
+            raise ValueError(f"batch_size must be >= 1, got {batch_size}")
+    if sparse_from_k is not None:
+        raise ValueError("sparse_from_k was removed: the miner keeps dense bitvectors at every level. Drop the argument.")
+    if not isinstance(prune_apriori, bool):
+        raise TypeError(f"prune_apriori must be bool, got {type(prune_apriori).__name__}")
+    if not prune_apriori:
+        raise ValueError("prune_apriori=False was removed: every candidate's (k-1)-subsets are tested. Drop the argument.")
+
+
+def _unsupported(**opts) -> None:
+    """Reject the routes and options outside this engine's path (one GPU, counting path only)."""
+    for name, (value, why) in opts.items():
+        if value:
+            raise ValueError(f"{name} is not supported by the GB300 counting engine: {why}")
+
+
+# ---- input: transactions -> CSR of frequent columns ------------------------------
+
+def _list_column(transactions, item_col: str) -> tuple[np.ndarray, np.ndarray, np.dtype]:
+    """(indptr int64, flat item values, their numpy dtype) of a transaction list column.
+
+    Accepts a polars DataFrame/LazyFrame or pyarrow Table (when installed), a
+    CSR object with ``indptr`` and ``items`` arrays, a dict ``{item_col: rows}``
+    or a list of item lists. Null lists are rows without items; null entries
+    are no items.
+    """
+    if hasattr(transactions, "indptr") and hasattr(transactions, "items") and not isinstance(transactions, dict):
+        indptr = np.asarray(transactions.indptr, dtype=np.int64)
+        flat = np.asarray(transactions.items)
+        if not np.issubdtype(flat.dtype, np.integer):
+            raise TypeError(f"items must be integer ids on the GPU route, got {flat.dtype}")
+        return indptr, flat, flat.dtype
+    if isinstance(transactions, dict):
+        return _python_rows(transactions[item_col])
+    if isinstance(transactions, (list, tuple)):
+        return _python_rows(transactions)
+    arr = None
+    if _pl is not None and isinstance(transactions, (_pl.DataFrame, _pl.LazyFrame)):
+        lf = transactions.lazy() if isinstance(transactions, _pl.DataFrame) else transactions
+        arr = lf.select(_pl.col(item_col)).collect().get_column(item_col).to_arrow()
+    elif pa is not None and isinstance(transactions, pa.Table):
+        arr = transactions.column(item_col)
+    if arr is None:
+        raise TypeError(f"transactions must be a DataFrame, pyarrow Table, CSR, dict or list of lists, "
+                        f"got {type(transactions).__name__}")
+    if isinstance(arr, pa.ChunkedArray):
+        arr = arr.combine_chunks()
+    if not (pa.types.is_list(arr.type) or pa.types.is_large_list(arr.type)):
+        raise TypeError(f"column {item_col!r} must be a list column, got {arr.type}")
+    if not pa.types.is_integer(arr.type.value_type):
+        raise TypeError(f"items must be integer ids on the GPU route, got {arr.type.value_type}")
+    offsets = np.asarray(arr.offsets.to_numpy(zero_copy_only=False), dtype=np.int64)
+    n = len(arr)
+    vals = arr.values.slice(offsets[0], offsets[-1] - offsets[0])
+    valid = np.ones(len(vals), dtype=bool)
+    if vals.null_count:
+        valid &= ~np.asarray(vals.is_null().to_numpy(zero_copy_only=False))
+    if arr.null_count:
+        valid &= np.repeat(~np.asarray(arr.is_null().to_numpy(zero_copy_only=False)), np.diff(offsets))
+    flat = np.asarray(vals.fill_null(0).to_numpy(zero_copy_only=False))
+    rid = np.repeat(np.arange(n, dtype=np.int64), np.diff(offsets))[valid]
+    indptr = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(np.bincount(rid, minlength=n), out=indptr[1:])
+    return indptr, flat[valid], flat.dtype
+
+
+def _python_rows(rows) -> tuple[np.ndarray, np.ndarray, np.dtype]:
+    rows = [[] if r is None else [x for x in r if x is not None] for r in rows]
+    indptr = np.zeros(len(rows) + 1, dtype=np.int64)
+    np.cumsum([len(r) for r in rows], out=indptr[1:])
+    flat_list = [x for r in rows for x in r]
+    if any(not isinstance(x, numbers.Integral) for x in flat_list):
+        raise TypeError("items must be integer ids on the GPU route")
+    big = any(x > np.iinfo(np.int64).max for x in flat_list)
+    flat = np.array(flat_list, dtype=np.uint64 if big else np.int64)
+    return indptr, flat, flat.dtype
+
+
+def _frequent_csr(indptr: np.ndarray, flat: np.ndarray, n_rows: int, mc: int):
+    """(row_ptr, column ids int32, items of the columns): rows deduplicated, columns = items with count >= mc."""
+    rid = np.repeat(np.arange(n_rows, dtype=np.int64), np.diff(indptr))
+    items, inv = np.unique(flat, return_inverse=True)
+    key = rid * max(1, len(items)) + inv
+    key = np.unique(key)
+    rid = key // max(1, len(items))
+    inv = key % max(1, len(items))
+    counts = np.bincount(inv, minlength=len(items))
+    keep = counts >= max(1, mc)
+    remap = np.cumsum(keep) - 1
+    sel = keep[inv]
+    cols = remap[inv[sel]].astype(np.int32)
+    rid = rid[sel]
+    row_ptr = np.zeros(n_rows + 1, dtype=np.int64)
+    np.cumsum(np.bincount(rid, minlength=n_rows), out=row_ptr[1:])
+    return row_ptr, cols, items[keep]
+
+
+def build_device_bitvecs(row_ptr: np.ndarray, cols: np.ndarray, n_cols: int, n_rows: int, device=None):
+    """Column bitvectors [n_cols, ceil(N/64)] (torch int64 view of uint64) built on the device by etm_build_bitvecs."""
+    import torch
+
+    from ._lib import check, load_library
+
+    lib = load_library()
+    dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+    ld = max(1, (n_rows + 63) // 64)
+    rp = torch.from_numpy(row_ptr.astype(np.int64)).to(dev)
+    ids = torch.from_numpy(cols.astype(np.int32)).to(dev) if len(cols) else torch.zeros(1, dtype=torch.int32, device=dev)
+    bv = torch.empty((max(n_cols, 1), ld), dtype=torch.int64, device=dev)
+    if len(row_ptr) != n_rows + 1 or (n_rows and np.any(np.diff(row_ptr) < 0)) or row_ptr[-1] != len(cols):
+        raise ValueError("row_ptr must be a non-decreasing [n_rows + 1] array ending at len(cols)")
+    check(lib.etm_build_bitvecs(rp.data_ptr(), ids.data_ptr(), len(cols), None, 0, n_rows, n_cols, ld, bv.data_ptr(),
+                                torch.cuda.current_stream().cuda_stream), "etm_build_bitvecs")
+    return bv[:n_cols]
+
+
+# ---- output ------------------------------------------------------------------------
+
+class ItemsetFrame:
+    """The result without polars or pyarrow: ``itemset`` as (offsets, values) arrays and ``support`` float64.
+
+    ``to_arrow()`` / ``to_polars()`` convert when those libraries are
+    installed; ``itemsets()`` gives the rows as tuples.
+    """
+
+    def __init__(self, offsets: np.ndarray, values: np.ndarray, support: np.ndarray):
+        self.offsets = offsets
+        self.values = values
+        self.support = support
+
+    def __len__(self) -> int:
+        return len(self.support)
+
+    @property
+    def item_dtype(self) -> np.dtype:
+        return self.values.dtype
+
+    def itemsets(self) -> list[tuple[int, ...]]:
+        v, o = self.values.tolist(), self.offsets.tolist()
+        return [tuple(v[o[i]:o[i + 1]]) for i in range(len(self))]
+
+    def to_arrow(self):
+        if pa is None:
+            raise ImportError("pyarrow is not installed")
+        item_type = pa.uint64() if self.values.dtype == np.uint64 else pa.int64()
+        itemset = pa.LargeListArray.from_arrays(pa.array(self.offsets, pa.int64()), pa.array(self.values, item_type))
+        return pa.table({"itemset": itemset, "support": pa.array(self.support, pa.float64())})
+
+    def to_polars(self):
+        if _pl is None:
+            raise ImportError("polars is not installed")
+        return _pl.from_arrow(self.to_arrow())
+
+    def __repr__(self) -> str:
+        return f"ItemsetFrame({len(self)} itemsets, items {self.values.dtype})"
+
+
+def _frame(levels: list[tuple[np.ndarray, np.ndarray]], n_rows: int, wide: bool):
+    """itemset (list of ascending ids: Int64, UInt64 kept) + support (count / N).
+
+    A polars DataFrame when polars is installed, else a pyarrow Table when
+    pyarrow is, else an ``ItemsetFrame``.
+    """
+    np_type = np.uint64 if wide else np.int64
+    flats, offs, sups = [], [np.zeros(1, dtype=np.int64)], []
+    total = 0
+    for items, counts in levels:
+        n, k = items.shape
+        if n == 0:
+            continue
+        flats.append(np.ascontiguousarray(items).astype(np_type).ravel())
+        offs.append(total + k * np.arange(1, n + 1, dtype=np.int64))
+        total += n * k
+        sups.append(np.asarray(counts, dtype=np.float64) / max(1, n_rows))
+    frame = ItemsetFrame(np.concatenate(offs), np.concatenate(flats) if flats else np.zeros(0, np_type),
+                         np.concatenate(sups) if sups else np.zeros(0))
+    if _pl is not None:
+        return frame.to_polars()
+    if pa is not None:
+        return frame.to_arrow()
+    return frame
+
+
+def result_pairs(result, n_rows: int) -> list[tuple[tuple[int, ...], int]]:
+    """A result (frame or (frame, session)) as sorted (itemset tuple, count) pairs; count = rint(support * N)."""
+    df = result[0] if isinstance(result, tuple) else result
+    if isinstance(df, ItemsetFrame):
+        sets, sup = df.itemsets(), df.support
+    else:
+        table = df if (pa is not None and isinstance(df, pa.Table)) else df.to_arrow()
+        sets = [tuple(s) for s in table.column("itemset").to_pylist()]
+        sup = np.asarray(table.column("support").to_numpy(), dtype=np.float64)
+    counts = np.rint(np.asarray(sup, dtype=np.float64) * n_rows).astype(np.int64)
+    out = [(tuple(int(x) for x in s), int(c)) for s, c in zip(sets, counts)]
+    out.sort(key=lambda t: (len(t[0]), t[0]))
+    return out
+
+
+def _array_facts(bv) -> tuple[tuple[int, ...], str, bool]:
+    """(shape, numpy typestr, C-contiguous) of a device array: a torch CUDA tensor or any
+    ``__cuda_array_interface__`` object (core/apriori.py:491-527 checks the same facts)."""
+    try:
+        import torch
+
+        if isinstance(bv, torch.Tensor):
+            if not bv.is_cuda:
+                raise TypeError("bitvecs_gpu must be a CUDA tensor")
+            typestr = {torch.uint64: "<u8", torch.int64: "<i8"}.get(bv.dtype, str(bv.dtype))
+            return tuple(bv.shape), typestr, bv.is_contiguous()
+    except ImportError:  # pragma: no cover
+        pass
+    cai = getattr(bv, "__cuda_array_interface__", None)
+    if cai is None:
+        raise TypeError(f"bitvecs_gpu must expose __cuda_array_interface__, got {type(bv).__name__}")
+    shape = tuple(cai["shape"])
+    strides = cai.get("strides")
+    contiguous = strides is None or (len(shape) == 2 and tuple(strides) == (shape[1] * 8, 8))
+    return shape, cai["typestr"], contiguous
+
+
+def _emit(out: MineOutput, col_items: np.ndarray):
+    levels = [(col_items[cols], counts) for cols, counts in out.host_levels()]
+    return _frame(levels, out.n_rows, col_items.dtype == np.uint64)
+
+
+def _session_from(out: MineOutput, session: ProfilingSession) -> None:
+    for s in out.stats:
+        session.record_phase(f"k{s.k}", s.ms, n_candidates=s.n_candidates, n_frequent=s.n_frequent,
+                             n_groups=s.n_groups, n_chunks=s.n_chunks)
+
+
+def apriori(
+    transactions=None,
+    min_support: float = 0.5,
+    max_length: int | None = None,
+    item_col: str = "items",
+    use_gpu: bool = False,
+    batch_size: int | None = 10_000,
+    profile: bool = False,
+    show_progress: bool = False,
+    warn_complexity: bool = True,
+    prune_equal_support: bool = False,
+    use_generator_pruning: bool = False,
+    prune_apriori: bool = True,
+    sparse: bool | None = None,
+    n_jobs: int = 1,
+    enable_length_filter: bool = True,
+    streaming: bool = False,
+    chunk_size: int = 10_000_000,
+    n_gpus: int = 1,
+    memory_budget_gb: float | None = None,
+    progress_callback=None,
+    level_callback=None,
+    gpu_resident: bool = False,
+    bitvecs: tuple | None = None,
+    output_dir: str | None = None,
+    resume_from_k: int | None = None,
+    max_ram_gb: float = 800.0,
+    max_vram_gb: float = 70.0,
+    sparse_from_k: int | str | None = None,
+    anchor_items: set | None = None,
+    *,
+    engine: Engine | None = None,
+) -> Any:
+    """Frequent itemsets (or free-sets) with exact counts, mined on one GB300.
+
+    Parameters mean what they mean on the reference's ``apriori``; see the
+    module docstring for the inputs served. ``engine`` (keyword only, an
+    extension) reuses an ``Engine`` and its device scratch across calls.
+    """
+    _validate_parameters(min_support, max_length, batch_size, sparse_from_k, prune_apriori)
+    if sparse is not None:
+        raise ValueError("sparse= was removed: no route reads it. Drop the argument.")
+    if gpu_resident:
+        raise ValueError("gpu_resident was removed: use_gpu=True (or bitvecs=) keeps candidates and counts on the GPU.")
+    _unsupported(
+        streaming=(streaming, "SON streaming is not this engine's path"),
+        output_dir=(output_dir is not None, "the per-level parquet flush is not built"),
+        resume_from_k=(resume_from_k is not None, "resume is not built"),
+        anchor_items=(anchor_items is not None, "anchor filtering is not built"),
+        memory_budget_gb=(memory_budget_gb is not None, "it only sizes SON chunks"),
+        n_gpus=(n_gpus != 1, "one GB300 per call; run independent calls per GPU"),
+    )
+    if bitvecs is None and not use_gpu:
+        raise ValueError("the GB300 engine serves the GPU route: pass use_gpu=True or bitvecs=")
+    session = ProfilingSession() if profile else None
+    eng = engine or Engine()
+
+    if bitvecs is not None:
+        if transactions is not None:
+            raise ValueError("Cannot provide both 'transactions' and 'bitvecs'.")
+        if not isinstance(bitvecs, tuple) or len(bitvecs) != 3:
+            raise ValueError("bitvecs must be a tuple of (bitvecs_gpu, col_to_item, n_transactions)")
+        bv, col_to_item, n_trans = bitvecs
+        shape, typestr, contiguous = _array_facts(bv)
+        if len(shape) != 2:
+            raise ValueError(f"bitvecs_gpu must be 2D (n_cols, n_u64s), got {len(shape)}D")
+        if isinstance(n_trans, bool) or not isinstance(n_trans, numbers.Integral) or n_trans < 0:
+            raise ValueError(f"n_transactions must be a non-negative integer, got {n_trans!r}")
+        expected = math.ceil(n_trans / 64)
+        if shape[1] != expected:
+            raise ValueError(f"bitvecs_gpu.shape[1] ({shape[1]}) must equal ceil(n_transactions/64) = {expected}")
+        if len(col_to_item) != shape[0]:
+            raise ValueError(f"col_to_item has {len(col_to_item)} keys but bitvecs_gpu has {shape[0]} columns")
+        if not all(isinstance(v, numbers.Integral) for v in col_to_item.values()):
+            raise ValueError("col_to_item must map every column to an integer item id")
+        if typestr not in ("<u8", "|u8") or not contiguous:
+            raise ValueError(f"bitvecs_gpu must be a C-contiguous uint64 array, got {typestr}, c_contiguous={contiguous}")
+        n_trans = int(n_trans)
+        if n_trans > np.iinfo(np.int32).max:
+            raise ValueError(f"n_transactions={n_trans:,} exceeds int32 max: the count arrays are int32")
+        vals = [int(col_to_item[c]) for c in range(shape[0])] if shape[0] else []
+        wide = any(v > np.iinfo(np.int64).max for v in vals)
+        col_items = np.array(vals, dtype=np.uint64 if wide else np.int64)
+        out = eng.mine(bv, n_trans, min_support, max_length, prune_equal_support=prune_equal_support,
+                       use_generator_pruning=use_generator_pruning, level_callback=level_callback,
+                       n_cols_logical=(max(col_to_item.keys()) + 1) if col_to_item else 0)
+        if warn_complexity and out.stats:
+            _warn_complexity(out.stats[0].n_frequent, min_support)
+        df = _emit(out, col_items)
+        if session is not None:
+            _session_from(out, session)
+        return (df, session) if profile else df
+
+    if transactions is None:
+        raise ValueError("Either 'transactions' or 'bitvecs' must be provided")
+    indptr, flat, kind = _list_column(transactions, item_col)
+    n_rows = len(indptr) - 1
+    if n_rows > np.iinfo(np.int32).max:
+        raise ValueError(f"n_transactions={n_rows:,} exceeds int32 max")
+    wide = np.dtype(kind) == np.uint64
+    mc = min_count(min_support, n_rows)
+    row_ptr, cols, items = _frequent_csr(indptr, flat, n_rows, mc)
+    if len(items) == 0:
+        df = _frame([], max(1, n_rows), wide)
+        return (df, session) if profile else df
+    bv = build_device_bitvecs(row_ptr, cols, len(items), n_rows)
+    max_tx = int(np.diff(indptr).max()) if n_rows else 0
+    eff = min(max_length, max_tx) if max_length else max_tx
+    out = eng.mine(bv, n_rows, min_support, eff if eff >= 1 else 1, prune_equal_support=prune_equal_support,
+                   use_generator_pruning=use_generator_pruning, level_callback=level_callback)
+    if warn_complexity and out.stats:
+        _warn_complexity(out.stats[0].n_frequent, min_support)
+    df = _emit(out, items.astype(np.uint64 if wide else np.int64))
+    if session is not None:
+        _session_from(out, session)
+    return (df, session) if profile else df

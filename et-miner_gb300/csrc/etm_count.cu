@@ -1,0 +1,240 @@
+// Support counting on CUDA cores: the tile-pair AND+popcount kernel (prefix
+// groups with many members, and K=2 as the one group of every frequent
+// column) and the warp-per-candidate kernel (small groups).
+//
+// Tile kernel: a persistent grid walks a list of tile-pairs (ti <= tj) of
+// 64 x 64 suffixes. Per 32-word slab it stages in shared memory the AND of
+// the group's prefix columns, the 64 "A" suffix rows ANDed with it and the 64
+// "B" suffix rows, all with 16-byte coalesced loads; each of the 256 threads
+// then accumulates a 4 x 4 block of pair counts from registers. A slab whose
+// prefix AND is zero is skipped. The A-row reads are (near) broadcasts and the
+// B rows are read at a padded 33-word stride, so the shared-memory reads are
+// free of bank conflicts.
+#include "etm_common.cuh"
+#include "etm_count.cuh"
+
+namespace {
+
+using namespace etm;
+
+constexpr int TT = 64;                 // suffixes per tile side
+constexpr int WCH = 32;                // words per shared-memory slab
+constexpr int TILE_THREADS = 256;      // 16 x 16 threads, 4 x 4 pairs each
+constexpr int MAXP = 63;               // prefix columns handled
+constexpr int STRIDE = WCH + 1;        // padded row stride (words)
+
+struct TileShared {
+    uint64_t a[TT * STRIDE];
+    uint64_t b[TT * STRIDE];
+    uint64_t pre[WCH];
+    int32_t sa[TT];
+    int32_t sb[TT];
+    int32_t pref[MAXP + 1];
+    int flag;
+};
+
+__global__ void __launch_bounds__(TILE_THREADS) count_tiles_popc_kernel(
+    const uint64_t* __restrict__ fbv, int64_t ld, int64_t n_words, const int32_t* __restrict__ rows, int width,
+    const int64_t* __restrict__ grp_first, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
+    const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
+    const uint8_t* __restrict__ cls, int32_t* __restrict__ out) {
+    __shared__ TileShared sh;
+    const int tid = threadIdx.x;
+    const int ty = tid >> 4, tx = tid & 15;
+    const int64_t total = work_off[n_work];
+    const int plen = width - 1;
+    const int64_t n_slabs = ceil_div<int64_t>(n_words, WCH);
+
+    for (int64_t tp = blockIdx.x; tp < total; tp += gridDim.x) {
+        const int64_t wi = upper_find(work_off, n_work, tp);
+        const int64_t g = work_groups[wi];
+        const int64_t m = grp_size[g];
+        const int64_t nt = ceil_div<int64_t>(m, TT);
+        int64_t ti, tj1;
+        tri_decode(tp - work_off[wi], nt + 1, &ti, &tj1);
+        const int64_t tj = tj1 - 1;
+        const int64_t first = grp_first[g];
+        const int64_t cb = cand_off[g] - chunk_base;
+
+        if (tid < TT) {
+            const int64_t ia = ti * TT + tid, ib = tj * TT + tid;
+            sh.sa[tid] = ia < m ? rows[(first + ia) * width + plen] : -1;
+            sh.sb[tid] = ib < m ? rows[(first + ib) * width + plen] : -1;
+        }
+        if (tid < plen) sh.pref[tid] = rows[first * width + tid];
+
+        // Candidates of this tile-pair that still need a count.
+        int any = cls == nullptr;
+        if (!any) {
+            for (int r = 0; r < 4 && !any; r++) {
+                const int64_t i = ti * TT + ty * 4 + r;
+                for (int c = 0; c < 4; c++) {
+                    const int64_t j = tj * TT + tx + 16 * c;
+                    if (i < j && j < m && cls[cb + tri_index(i, j, m)] == ETM_CAND_COUNT) {
+                        any = 1;
+                        break;
+                    }
+                }
+            }
+        }
+        if (!__syncthreads_or(any)) continue;
+
+        unsigned acc[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) acc[r][c] = 0;
+
+        for (int64_t s = 0; s < n_slabs; s++) {
+            const int64_t w0 = s * WCH;
+            if (tid < WCH) {
+                uint64_t p = ~0ULL;
+                for (int q = 0; q < plen; q++) p &= __ldg(fbv + (int64_t)sh.pref[q] * ld + w0 + tid);
+                sh.pre[tid] = p;
+            }
+            __syncthreads();
+            const int live = tid < WCH ? (sh.pre[tid] != 0ULL) : 0;
+            if (!__syncthreads_or(live)) continue;
+            // Stage A (masked by the prefix) and B: 64 rows x 16 vectors each.
+#pragma unroll
+            for (int q = 0; q < (TT * WCH / 2) / TILE_THREADS; q++) {
+                const int idx = q * TILE_THREADS + tid;
+                const int r = idx >> 4, v = idx & 15;
+                const int ca = sh.sa[r], cbb = sh.sb[r];
+                ulonglong2 xa = make_ulonglong2(0, 0), xb = make_ulonglong2(0, 0);
+                if (ca >= 0) xa = __ldg(reinterpret_cast<const ulonglong2*>(fbv + (int64_t)ca * ld + w0) + v);
+                if (cbb >= 0) xb = __ldg(reinterpret_cast<const ulonglong2*>(fbv + (int64_t)cbb * ld + w0) + v);
+                sh.a[r * STRIDE + 2 * v] = xa.x & sh.pre[2 * v];
+                sh.a[r * STRIDE + 2 * v + 1] = xa.y & sh.pre[2 * v + 1];
+                sh.b[r * STRIDE + 2 * v] = xb.x;
+                sh.b[r * STRIDE + 2 * v + 1] = xb.y;
+            }
+            __syncthreads();
+#pragma unroll 4
+            for (int w = 0; w < WCH; w++) {
+                uint64_t av[4], bv[4];
+#pragma unroll
+                for (int r = 0; r < 4; r++) av[r] = sh.a[(ty * 4 + r) * STRIDE + w];
+#pragma unroll
+                for (int c = 0; c < 4; c++) bv[c] = sh.b[(tx + 16 * c) * STRIDE + w];
+#pragma unroll
+                for (int r = 0; r < 4; r++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) acc[r][c] += __popcll(av[r] & bv[c]);
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const int64_t i = ti * TT + ty * 4 + r;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const int64_t j = tj * TT + tx + 16 * c;
+                if (i < j && j < m) {
+                    const int64_t t = cb + tri_index(i, j, m);
+                    if (cls == nullptr || cls[t] == ETM_CAND_COUNT) out[t] = (int32_t)acc[r][c];
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+constexpr int CAND_THREADS = 256;
+constexpr int MAXK = 64;
+
+// One warp per candidate: AND of its k columns, 16 bytes per lane per step.
+// The candidate's columns sit in the warp's slice of shared memory, so the
+// word loop (whose trip count differs between lanes) holds no warp collective.
+__global__ void __launch_bounds__(CAND_THREADS) count_cands_kernel(
+    const uint64_t* __restrict__ fbv, int64_t ld, int64_t n_words, const int32_t* __restrict__ rows, int width,
+    const int64_t* __restrict__ grp_first, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
+    const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
+    const uint8_t* __restrict__ cls, int32_t* __restrict__ out) {
+    __shared__ int32_t cols_sh[CAND_THREADS / 32][MAXK];
+    const int lane = threadIdx.x & 31;
+    int32_t* cols = cols_sh[threadIdx.x >> 5];
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t total = work_off[n_work];
+    const int64_t n_vec = (n_words + 1) >> 1;
+    const int k = width + 1;
+    for (int64_t c = warp; c < total; c += n_warps) {
+        const int64_t wi = upper_find(work_off, n_work, c);
+        const int64_t g = work_groups[wi];
+        const int64_t local = c - work_off[wi];
+        const int64_t t = cand_off[g] - chunk_base + local;
+        if (cls && cls[t] != ETM_CAND_COUNT) continue;  // warp-uniform: every lane has the same c
+        int64_t i, j;
+        tri_decode(local, grp_size[g], &i, &j);
+        const int64_t first = grp_first[g];
+        __syncwarp();
+        for (int q = lane; q < k; q += 32)
+            cols[q] = q < width ? rows[(first + i) * width + q] : rows[(first + j) * width + width - 1];
+        __syncwarp();
+        unsigned s = 0;
+        for (int64_t v = lane; v < n_vec; v += 32) {
+            ulonglong2 x = __ldg(reinterpret_cast<const ulonglong2*>(fbv + (int64_t)cols[0] * ld) + v);
+            for (int q = 1; q < k; q++) {
+                const ulonglong2 y = __ldg(reinterpret_cast<const ulonglong2*>(fbv + (int64_t)cols[q] * ld) + v);
+                x.x &= y.x;
+                x.y &= y.y;
+            }
+            s += __popcll(x.x) + __popcll(x.y);
+        }
+        s = __reduce_add_sync(0xffffffffu, s);
+        if (lane == 0) out[t] = (int32_t)s;
+    }
+}
+
+}  // namespace
+
+namespace etm {
+
+int count_tiles_popcount(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                         const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
+                         const int64_t* work_groups, const int64_t* work_off, int64_t n_work, int64_t chunk_base,
+                         const uint8_t* cls, int32_t* out, int64_t n_tiles_hint, cudaStream_t s) {
+    const int64_t cap = (int64_t)max(1, sm_count()) * 6;
+    const int grid = (int)max64(1, min(cap, n_tiles_hint > 0 ? n_tiles_hint : cap));
+    count_tiles_popc_kernel<<<grid, TILE_THREADS, 0, s>>>(fbv, ld, n_words, rows, width, grp_first, grp_size, cand_off,
+                                                          work_groups, work_off, n_work, chunk_base, cls, out);
+    ETM_LAUNCHED("count_tiles_popc");
+    return ETM_OK;
+}
+
+}  // namespace etm
+
+extern "C" int etm_count_tiles(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                               const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
+                               const int64_t* work_groups, const int64_t* work_off, int64_t n_work,
+                               int64_t chunk_base, const uint8_t* cls, int32_t method, int32_t* out_counts,
+                               void* stream) {
+    ETM_REQUIRE(width >= 1 && width <= MAXP, ETM_EINVAL, "etm_count_tiles: width %d out of range", width);
+    ETM_REQUIRE(ld % WCH == 0 && ld >= n_words, ETM_EINVAL, "etm_count_tiles: ld must be a multiple of %d >= n_words", WCH);
+    ETM_REQUIRE((reinterpret_cast<uintptr_t>(fbv) & 15) == 0, ETM_EINVAL, "etm_count_tiles: fbv must be 16-byte aligned");
+    if (n_work <= 0) return ETM_OK;
+    cudaStream_t s = as_stream(stream);
+    if (method == ETM_METHOD_TENSOR)
+        return etm::count_tiles_tensor(fbv, ld, n_words, rows, width, grp_first, grp_size, cand_off, work_groups,
+                                       work_off, n_work, chunk_base, cls, out_counts, s);
+    ETM_REQUIRE(method == ETM_METHOD_POPCOUNT, ETM_EINVAL, "etm_count_tiles: unknown method %d", method);
+    return etm::count_tiles_popcount(fbv, ld, n_words, rows, width, grp_first, grp_size, cand_off, work_groups,
+                                     work_off, n_work, chunk_base, cls, out_counts, -1, s);
+}
+
+extern "C" int etm_count_cands(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                               const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
+                               const int64_t* work_groups, const int64_t* work_off, int64_t n_work,
+                               int64_t chunk_base, const uint8_t* cls, int32_t* out_counts, void* stream) {
+    ETM_REQUIRE(width >= 1 && width < MAXK, ETM_EINVAL, "etm_count_cands: width %d out of range", width);
+    ETM_REQUIRE(ld % 2 == 0 && ld >= n_words, ETM_EINVAL, "etm_count_cands: ld must be even and >= n_words");
+    ETM_REQUIRE((reinterpret_cast<uintptr_t>(fbv) & 15) == 0, ETM_EINVAL, "etm_count_cands: fbv must be 16-byte aligned");
+    if (n_work <= 0) return ETM_OK;
+    const int grid = max(1, sm_count()) * 8;
+    count_cands_kernel<<<grid, CAND_THREADS, 0, as_stream(stream)>>>(fbv, ld, n_words, rows, width, grp_first, grp_size,
+                                                                     cand_off, work_groups, work_off, n_work,
+                                                                     chunk_base, cls, out_counts);
+    ETM_LAUNCHED("count_cands");
+    return ETM_OK;
+}

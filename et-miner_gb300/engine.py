@@ -1,0 +1,442 @@
+"""The level driver: ET-Miner's GPU mining loop on one GB300, over the C-ABI library.
+
+Restates the behaviour of ``_apriori_row_split_multi_gpu``
+(gpu/row_split.py:229-1185) for one device: K=1 popcounts and the free
+items, then level by level the prefix groups of the generating level, the
+subset test / count inference, the counting kernels, the survivor
+compaction and the free-set test. Every step runs on the device; the host
+only plans candidate chunks from the group sizes and reads the totals it
+needs to size the next allocation.
+
+Differences from the reference's internals (results are identical):
+
+* The level's itemsets never leave the device between levels: candidates
+  are decoded into the next level's rows by the compaction kernel, already in
+  lexicographic order, so there is no host decode, lexsort or group build.
+* Levels are held in "generator index" space: column ids 0..n_g-1 index the
+  engine's padded copy of the generating columns (``fbv``); results map back
+  to the caller's columns through ``gen_cols``.
+
+Forms:
+    "batched"  one launch per candidate chunk and kernel kind (default)
+    "plain"    one counting launch per prefix group: the one-launch-per-group
+               comparator the batched form is measured against
+"""
+
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+from fractions import Fraction
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, load_library
+
+#: A prefix group with at most this many members is counted one warp per candidate.
+SMALL_GROUP = 16
+#: Suffixes per tile side of the tile-pair kernel.
+TILE = 64
+#: Candidates per chunk (int32 count + uint8 class each): bounds the level's dense scratch.
+CHUNK_CANDS = 1 << 27
+#: Counting method for tile-pairs: "popcount" or "tensor".
+DEFAULT_METHOD = "popcount"
+
+
+def min_count(min_support: float, n_rows: int) -> int:
+    """ceil(s * N), s read as its shortest round-tripping decimal (core/result.py:57-79)."""
+    return math.ceil(Fraction(str(min_support)) * n_rows)
+
+
+def mining_min_count(min_support: float, n_rows: int) -> int:
+    """The threshold the levels apply: ``min_count``, at least 1, as the CPU route does
+    (core/cpu_miner.py:967-970); at 0 every pair would be "frequent" with count 0."""
+    return max(1, min_count(min_support, n_rows))
+
+
+def _p(t: torch.Tensor | None) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+@dataclass
+class Level:
+    """One level on the device: rows int32 [n, k] in generator-index space, counts int32 [n], free flags."""
+
+    rows: torch.Tensor
+    counts: torch.Tensor
+    free: torch.Tensor | None = None
+
+    @property
+    def n(self) -> int:
+        return int(self.rows.shape[0])
+
+    @property
+    def k(self) -> int:
+        return int(self.rows.shape[1])
+
+
+@dataclass
+class LevelStats:
+    k: int
+    n_candidates: int
+    n_frequent: int
+    ms: float
+    n_groups: int = 0
+    n_chunks: int = 0
+    launches: int = 0
+
+
+@dataclass
+class MineOutput:
+    """Emitted levels (device tensors in generator-index space) and how to map them back.
+
+    ``gen_cols[g]`` is the caller's column of generator index g. Level 1 is
+    held as the caller's columns directly (``level1_cols``) because under the
+    free-set prune it differs from the generators only by nothing, and in a
+    complete run every frequent column is both.
+    """
+
+    n_rows: int
+    min_count: int
+    gen_cols: np.ndarray
+    level1_cols: np.ndarray
+    level1_counts: np.ndarray
+    levels: list[Level] = field(default_factory=list)
+    stats: list[LevelStats] = field(default_factory=list)
+
+    def host_levels(self) -> list[tuple[np.ndarray, np.ndarray]]:
+        """Every emitted level as (caller column ids int64 [n, k], counts int64 [n]) on the host."""
+        out = []
+        if len(self.level1_cols):
+            out.append((self.level1_cols[:, None].astype(np.int64), self.level1_counts.astype(np.int64)))
+        for lv in self.levels:
+            if lv.n == 0:
+                continue
+            rows = lv.rows.cpu().numpy()
+            out.append((self.gen_cols[rows].astype(np.int64), lv.counts.cpu().numpy().astype(np.int64)))
+        return out
+
+    def n_itemsets(self) -> int:
+        return len(self.level1_cols) + sum(lv.n for lv in self.levels)
+
+
+class _Scratch:
+    """Reusable device buffers, grown on demand (torch allocations: plumbing only)."""
+
+    def __init__(self, device: torch.device):
+        self.device = device
+        self.bufs: dict[str, torch.Tensor] = {}
+
+    def get(self, name: str, n: int, dtype: torch.dtype) -> torch.Tensor:
+        t = self.bufs.get(name)
+        n = max(int(n), 1)
+        if t is None or t.dtype != dtype or t.numel() < n:
+            t = torch.empty(int(n * 1.25) + 16, dtype=dtype, device=self.device)
+            self.bufs[name] = t
+        return t[:n]
+
+
+def scan_words(n: int) -> int:
+    return (max(n, 1) + 4095) // 4096 + 2
+
+
+def as_device_bitvecs(bitvecs) -> tuple[int, tuple[int, int], object]:
+    """(device pointer, (n_cols, n_words), owner) of a C-contiguous uint64 device array.
+
+    Accepts a torch CUDA tensor (uint64 or int64) or any object exposing
+    ``__cuda_array_interface__`` with typestr ``<u8``.
+    """
+    if isinstance(bitvecs, torch.Tensor):
+        if not bitvecs.is_cuda:
+            raise TypeError("bitvecs must live on a CUDA device")
+        if bitvecs.dtype not in (torch.uint64, torch.int64):
+            raise ValueError(f"bitvecs must be uint64, got {bitvecs.dtype}")
+        if bitvecs.dim() != 2 or not bitvecs.is_contiguous():
+            raise ValueError("bitvecs must be a C-contiguous 2-D array")
+        return bitvecs.data_ptr(), (int(bitvecs.shape[0]), int(bitvecs.shape[1])), bitvecs
+    cai = getattr(bitvecs, "__cuda_array_interface__", None)
+    if cai is None:
+        raise TypeError(f"bitvecs must expose __cuda_array_interface__, got {type(bitvecs).__name__}")
+    shape = tuple(cai["shape"])
+    if len(shape) != 2:
+        raise ValueError(f"bitvecs must be 2D (n_cols, n_u64s), got {len(shape)}D")
+    if cai["typestr"] not in ("<u8", "|u8"):
+        raise ValueError(f"bitvecs must be uint64, got {cai['typestr']}")
+    strides = cai.get("strides")
+    if strides is not None and tuple(strides) != (shape[1] * 8, 8):
+        raise ValueError("bitvecs must be C-contiguous")
+    return int(cai["data"][0]), (int(shape[0]), int(shape[1])), bitvecs
+
+
+class Engine:
+    """One device's mining state: the library, scratch buffers and the counting choices."""
+
+    def __init__(self, device: torch.device | int | None = None, *, method: str = DEFAULT_METHOD,
+                 form: str = "batched", chunk_cands: int = CHUNK_CANDS, small_group: int = SMALL_GROUP):
+        if not torch.cuda.is_available():
+            raise RuntimeError("the GB300 engine needs a CUDA device; there is no CPU fallback")
+        self.lib = load_library()
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else
+                                   (device.index if isinstance(device, torch.device) else int(device)))
+        if method not in ("popcount", "tensor"):
+            raise ValueError(f"method must be 'popcount' or 'tensor', got {method!r}")
+        if form not in ("batched", "plain"):
+            raise ValueError(f"form must be 'batched' or 'plain', got {form!r}")
+        self.method = method
+        self.form = form
+        self.chunk_cands = int(chunk_cands)
+        self.small_group = int(small_group)
+        self.scratch = _Scratch(self.device)
+        self.launches = 0
+        #: When set, every counting / compaction launch is bracketed by CUDA events on its stream.
+        self.profile_kernels = False
+        self._events: list[tuple[str, object, object, int]] = []
+
+    # -- kernel timing ----------------------------------------------------------
+    def _launch(self, name: str, nbytes: int, fn):
+        """Run ``fn`` (one library call), timing it with CUDA events when profiling."""
+        if not self.profile_kernels:
+            return fn()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        st = fn()
+        e1.record()
+        self._events.append((name, e0, e1, int(nbytes)))
+        return st
+
+    def reset_kernel_times(self) -> None:
+        self._events = []
+
+    def kernel_report(self) -> dict:
+        """Per kernel: launches, total ms (CUDA events on the launching stream), algorithmic bytes."""
+        torch.cuda.synchronize()
+        out: dict[str, dict] = {}
+        for name, e0, e1, nbytes in self._events:
+            r = out.setdefault(name, {"name": name, "launches": 0, "ms": 0.0, "bytes": 0})
+            r["launches"] += 1
+            r["ms"] += e0.elapsed_time(e1)
+            r["bytes"] += nbytes
+        for r in out.values():
+            r["gbs"] = r["bytes"] / (r["ms"] / 1e3) / 1e9 if r["ms"] > 0 else 0.0
+        return out
+
+    # -- K = 1 -----------------------------------------------------------------
+    def column_counts(self, ptr: int, n_cols: int, n_words: int, ld: int) -> np.ndarray:
+        out = self.scratch.get("colcounts", n_cols, torch.int64)
+        check(self.lib.etm_popcount_cols(ptr, n_cols, n_words, ld, _p(out), _stream()), "etm_popcount_cols")
+        self.launches += 1
+        return out.cpu().numpy().copy()
+
+    def gather(self, ptr: int, ld: int, cols: np.ndarray, n_words: int) -> tuple[torch.Tensor, int]:
+        ldp = max(32, (n_words + 31) // 32 * 32)
+        fbv = torch.empty((max(len(cols), 1), ldp), dtype=torch.int64, device=self.device)
+        cols_d = torch.from_numpy(cols.astype(np.int32)).to(self.device)
+        check(self.lib.etm_gather_cols(ptr, ld, _p(cols_d), len(cols), n_words, _p(fbv), ldp, _stream()),
+              "etm_gather_cols")
+        self.launches += 1
+        return fbv, ldp
+
+    # -- K >= 2 ----------------------------------------------------------------
+    def groups(self, gen: Level):
+        n, width = gen.n, gen.k
+        grp_first = self.scratch.get("grp_first", n, torch.int64)
+        grp_size = self.scratch.get("grp_size", n, torch.int32)
+        cand_off = self.scratch.get("cand_off", n + 1, torch.int64)
+        counters = self.scratch.get("counters", 2, torch.int64)
+        ws = self.scratch.get("ws_groups", 3 + scan_words(n), torch.int64)
+        check(self.lib.etm_level_groups(_p(gen.rows), n, width, _p(grp_first), _p(grp_size), _p(cand_off),
+                                        _p(counters), _p(ws), ws.numel(), _stream()), "etm_level_groups")
+        self.launches += 10
+        G, total = (int(x) for x in counters.cpu().tolist())
+        return G, total, grp_first, grp_size, cand_off
+
+    def _work(self, ids: np.ndarray, weights: np.ndarray) -> tuple[torch.Tensor, torch.Tensor]:
+        off = np.zeros(len(ids) + 1, dtype=np.int64)
+        np.cumsum(weights, out=off[1:])
+        both = torch.from_numpy(np.concatenate([ids.astype(np.int64), off])).to(self.device, non_blocking=False)
+        return both[: len(ids)], both[len(ids):]
+
+    def count_level(self, gen: Level, fbv: torch.Tensor, ldp: int, n_words: int, mc: int,
+                    infer: bool, prune: bool) -> tuple[Level, LevelStats]:
+        """Count every candidate of the level generated by ``gen``; returns the survivors (k = gen.k + 1)."""
+        t0 = time.perf_counter()
+        width = gen.k
+        G, total, grp_first, grp_size, cand_off = self.groups(gen)
+        stats = LevelStats(width + 1, total, 0, 0.0, G)
+        out_rows = torch.empty((0, width + 1), dtype=torch.int32, device=self.device)
+        out_counts = torch.empty(0, dtype=torch.int32, device=self.device)
+        if total == 0:
+            stats.ms = (time.perf_counter() - t0) * 1e3
+            return Level(out_rows, out_counts), stats
+        sizes = grp_size[:G].cpu().numpy().astype(np.int64)
+        offs = cand_off[: G + 1].cpu().numpy()
+        # The subset test has prefix subsets to look up only from K=3 on.
+        classify = (infer or prune) and width >= 2
+        mode = (1 if prune or infer else 0) | (2 if infer else 0)
+        cap = int(min(total, max(1 << 16, 2 * gen.n)))
+        out_rows = torch.empty((cap, width + 1), dtype=torch.int32, device=self.device)
+        out_counts = torch.empty(cap, dtype=torch.int32, device=self.device)
+        acc = self.scratch.get("acc", 1, torch.int64)
+        acc.zero_()
+        n_out = 0
+        method = 1 if self.method == "tensor" else 0
+        g0 = 0
+        while g0 < G:
+            # Chunk: whole groups whose candidates fit the budget (at least one group).
+            limit = offs[g0] + max(self.chunk_cands, int(offs[g0 + 1] - offs[g0]))
+            g1 = int(np.searchsorted(offs, limit, side="right")) - 1
+            g1 = max(g1, g0 + 1)
+            base = int(offs[g0])
+            n_c = int(offs[g1] - base)
+            counts = self.scratch.get("chunk_counts", n_c, torch.int32)
+            cls = self.scratch.get("chunk_cls", n_c, torch.uint8) if classify else None
+            if classify:
+                check(self.lib.etm_classify(_p(gen.rows), width, gen.n, _p(gen.counts), _p(gen.free),
+                                            _p(grp_first), _p(grp_size), _p(cand_off), g0, g1, mode, _p(cls),
+                                            _p(counts), _stream()), "etm_classify")
+                self.launches += 1
+            m = sizes[g0:g1]
+            ids = np.arange(g0, g1, dtype=np.int64)
+            small = m <= self.small_group
+            for kind, sel in (("cands", small), ("tiles", ~small)):
+                gids = ids[sel]
+                if len(gids) == 0:
+                    continue
+                if kind == "cands":
+                    w = m[sel] * (m[sel] - 1) // 2
+                else:
+                    nt = (m[sel] + TILE - 1) // TILE
+                    w = nt * (nt + 1) // 2
+                batches = [(gids, w)] if self.form == "batched" else [(gids[q:q + 1], w[q:q + 1]) for q in range(len(gids))]
+                for bg, bw in batches:
+                    wg, wo = self._work(bg, bw)
+                    mg = sizes[bg]
+                    if kind == "cands":
+                        # Every candidate reads its k columns.
+                        nbytes = int((mg * (mg - 1) // 2).sum()) * (width + 1) * n_words * 8
+                        st = self._launch("count_cands", nbytes, lambda: self.lib.etm_count_cands(
+                            _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
+                            _p(wg), _p(wo), len(bg), base, _p(cls), _p(counts), _stream()))
+                    else:
+                        # Each group's prefix and suffix columns, once (the same-data minimum).
+                        nbytes = int((mg + width - 1).sum()) * n_words * 8
+                        st = self._launch("count_tiles", nbytes, lambda: self.lib.etm_count_tiles(
+                            _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
+                            _p(wg), _p(wo), len(bg), base, _p(cls), method, _p(counts), _stream()))
+                    check(st, f"etm_count_{kind}")
+                    self.launches += 1
+            ws = self.scratch.get("ws_compact", scan_words(n_c), torch.int64)
+            while True:
+                st = self._launch("level_compact", n_c * (5 if classify else 4), lambda: self.lib.etm_level_compact(
+                    _p(counts), _p(cls), n_c, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off), g0, g1,
+                    mc, _p(out_rows), _p(out_counts), cap, _p(acc), _p(ws), ws.numel(), _stream()))
+                check(st, "etm_level_compact")
+                self.launches += 3
+                new_total = int(acc.item())
+                if new_total <= cap:
+                    break
+                cap = int(min(total, max(2 * cap, int(new_total * 1.25))))
+                grown_r = torch.empty((cap, width + 1), dtype=torch.int32, device=self.device)
+                grown_c = torch.empty(cap, dtype=torch.int32, device=self.device)
+                grown_r[:n_out] = out_rows[:n_out]
+                grown_c[:n_out] = out_counts[:n_out]
+                out_rows, out_counts = grown_r, grown_c
+                acc.fill_(n_out)
+            n_out = new_total
+            stats.n_chunks += 1
+            g0 = g1
+        level = Level(out_rows[:n_out], out_counts[:n_out])
+        stats.n_frequent = n_out
+        stats.ms = (time.perf_counter() - t0) * 1e3
+        return level, stats
+
+    def finish_level(self, new: Level, gen: Level, track_free: bool, prune: bool) -> Level:
+        """Free flags against the generating level; under the free-set prune keep the free rows
+        whose subsets are all generators (gpu/row_split.py:1075-1100)."""
+        if not track_free or new.n == 0:
+            if track_free:
+                new.free = torch.zeros(0, dtype=torch.uint8, device=self.device)
+            return new
+        free = torch.empty(new.n, dtype=torch.uint8, device=self.device)
+        present = torch.empty(new.n, dtype=torch.uint8, device=self.device) if prune else None
+        check(self.lib.etm_level_subsets(_p(new.rows), _p(new.counts), new.n, gen.k, _p(gen.rows), _p(gen.counts),
+                                         gen.n, _p(free), _p(present), _stream()), "etm_level_subsets")
+        self.launches += 1
+        if not prune:
+            new.free = free
+            return new
+        out_r = torch.empty_like(new.rows)
+        out_c = torch.empty_like(new.counts)
+        out_f = torch.empty_like(free)
+        acc = self.scratch.get("acc_sel", 1, torch.int64)
+        acc.zero_()
+        ws = self.scratch.get("ws_select", scan_words(new.n), torch.int64)
+        check(self.lib.etm_select_rows(_p(new.rows), _p(new.counts), _p(free), _p(present), new.n, new.k, _p(out_r),
+                                       _p(out_c), _p(free), _p(out_f), new.n, _p(acc), _p(ws), ws.numel(),
+                                       _stream()), "etm_select_rows")
+        self.launches += 3
+        kept = int(acc.item())
+        return Level(out_r[:kept], out_c[:kept], out_f[:kept])
+
+    # -- the whole mine ----------------------------------------------------------
+    def mine(self, bitvecs, n_rows: int, min_support: float, max_length: int | None = None, *,
+             prune_equal_support: bool = False, use_generator_pruning: bool = False,
+             level_callback=None, n_cols_logical: int | None = None) -> MineOutput:
+        ptr, (n_cols, ld), _owner = as_device_bitvecs(bitvecs)
+        if n_rows >= 2**31:
+            raise ValueError(f"n_transactions={n_rows:,} exceeds int32 max: the count arrays are int32")
+        n_words = (n_rows + 63) // 64
+        if ld < n_words:
+            raise ValueError(f"bitvecs has {ld} words per column, fewer than ceil({n_rows}/64)")
+        mc = mining_min_count(min_support, n_rows)
+        prune, infer = bool(prune_equal_support), bool(use_generator_pruning) and not prune_equal_support
+        track_free = prune or bool(use_generator_pruning)
+        t0 = time.perf_counter()
+        col_counts = self.column_counts(ptr, n_cols, n_words, ld) if n_cols else np.zeros(0, np.int64)
+        freq = np.flatnonzero(col_counts >= mc)
+        free1 = col_counts[freq] < n_rows
+        gen_cols = freq[free1] if prune else freq
+        out = MineOutput(n_rows, mc, gen_cols.astype(np.int64), gen_cols.astype(np.int64),
+                         col_counts[gen_cols].astype(np.int64))
+        out.stats.append(LevelStats(1, n_cols, len(gen_cols), (time.perf_counter() - t0) * 1e3))
+        if level_callback:
+            level_callback(1, n_cols, len(gen_cols), out.stats[-1].ms)
+        n_logical = n_cols if n_cols_logical is None else n_cols_logical
+        max_k = min(max_length if max_length else n_logical, n_logical)
+        if len(gen_cols) < 2 or max_k < 2:
+            return out
+        fbv, ldp = self.gather(ptr, ld, gen_cols, n_words)
+        ng = len(gen_cols)
+        gen = Level(torch.arange(ng, dtype=torch.int32, device=self.device)[:, None].contiguous(),
+                    torch.from_numpy(col_counts[gen_cols].astype(np.int32)).to(self.device),
+                    torch.from_numpy(free1[free1] if prune else free1).to(self.device).to(torch.uint8))
+        k = 2
+        while k <= max_k and gen.n >= k:
+            t_level = time.perf_counter()
+            new, stats = self.count_level(gen, fbv, ldp, n_words, mc, infer, prune)
+            new = self.finish_level(new, gen, track_free, prune)
+            stats.n_frequent = new.n
+            stats.ms = (time.perf_counter() - t_level) * 1e3
+            out.stats.append(stats)
+            if level_callback:
+                level_callback(k, stats.n_candidates, new.n, stats.ms)
+            if new.n == 0:
+                break
+            out.levels.append(new)
+            gen = new
+            k += 1
+        return out
+
+
+def mine(bitvecs, n_rows: int, min_support: float, max_length: int | None = None, **kw) -> MineOutput:
+    """Mine device bitvectors [n_cols, ceil(N/64)] with a fresh ``Engine`` (see ``Engine.mine``)."""
+    engine_kw = {k: kw.pop(k) for k in ("method", "form", "chunk_cands", "small_group", "device") if k in kw}
+    return Engine(**engine_kw).mine(bitvecs, n_rows, min_support, max_length, **kw)

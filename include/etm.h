@@ -1,0 +1,194 @@
+/*
+ * libetm_gb300 — C ABI of the GB300 exact Apriori counting engine.
+ *
+ * Drop-in boundary for ET-Miner's GPU counting path (the level driver
+ * `_apriori_row_split_multi_gpu`, gpu/row_split.py:229-1185, reached from
+ * `apriori(..., use_gpu=True, bitvecs=...)`, core/apriori.py:477-548).
+ *
+ * Every entry point takes device pointers, plain sizes and a CUDA stream
+ * (cudaStream_t passed as void*, NULL = legacy default stream), enqueues its
+ * work on that stream and returns a status (ETM_OK = 0). On failure
+ * etm_last_error() describes it. No entry point allocates device memory
+ * except where it says so: scratch is passed in as `ws` (int64 words) with its
+ * size, and each function states how many words it needs.
+ *
+ * Data conventions (core/apriori.py:409-413, csr_to_bitvec.cu:27-35):
+ *   bitvectors   uint64 [n_cols][ld]; bit r%64 of word r/64 of column c is set
+ *                when transaction r holds column c; bits past N are zero.
+ *   level rows   int32 [n][width], column indices ascending within a row,
+ *                rows in strictly ascending lexicographic order.
+ *   counts       int32 (N < 2^31, gpu/row_split.py:358-362).
+ *   candidates   of a prefix group with m members (rows first..first+m-1
+ *                sharing their first width-1 columns): the C(m,2) pairs
+ *                (i < j), item list = prefix + s_i + s_j, in lexicographic
+ *                (i-major) order; a level's candidates are the groups' in order.
+ */
+#ifndef ETM_H
+#define ETM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ETM_OK 0
+#define ETM_EINVAL 1   /* bad argument: sizes, alignment, widths */
+#define ETM_ECUDA 2    /* a CUDA call or launch failed */
+#define ETM_ENOSPACE 3 /* workspace or output capacity too small */
+#define ETM_ETIMEOUT 4 /* a bounded device wait gave up */
+
+/* Candidate classes written by etm_classify (gpu/kernels/_src/_subset_index.cu:27-33). */
+#define ETM_CAND_COUNT 0
+#define ETM_CAND_SKIP 1
+#define ETM_CAND_INFER 2
+
+/* Mode bits of etm_classify (gpu/kernels/subset_index.py SUBSET_PRUNE / SUBSET_INFER). */
+#define ETM_SUBSET_PRUNE 1
+#define ETM_SUBSET_INFER 2
+
+/* Count methods of etm_pair_counts / etm_count_tiles. */
+#define ETM_METHOD_POPCOUNT 0 /* AND + popcount on CUDA cores */
+#define ETM_METHOD_TENSOR 1   /* 0/1 Gram on tcgen05 tensor cores, f32 accumulation in TMEM, exact */
+
+int etm_version(void);
+/* Message of the last failing call on this thread (empty if none). */
+const char* etm_last_error(void);
+/* SM count of the current device. */
+int etm_device_sm_count(void);
+
+/*
+ * CSR -> column bitvectors. Replaces csr_to_bitvec and ids_to_bitvec
+ * (gpu/kernels/_src/csr_to_bitvec.cu:9-73) and their drivers
+ * (gpu/csr_bitvec.py:63-155, gpu/input_layer.py:434-466).
+ * row_ptr int64 [n_rows+1], non-decreasing; ids int32 [nnz]; lut int32
+ * [lut_size] maps an id to its column or -1 (NULL: ids are columns). Ids
+ * outside the lut, columns outside [0, n_cols) and entries outside [0, nnz)
+ * are ignored. out_bv [n_cols][ld] is zeroed here, then filled.
+ * ld >= ceil(n_rows/64).
+ */
+int etm_build_bitvecs(const int64_t* row_ptr, const int32_t* ids, int64_t nnz, const int32_t* lut,
+                      int64_t lut_size, int64_t n_rows, int64_t n_cols, int64_t ld, uint64_t* out_bv, void* stream);
+
+/*
+ * K=1 support: popcount of each column over words [0, n_words). Replaces
+ * column_popcounts (gpu/kernels/loader.py:241-257) and the K=1 step of
+ * gpu/row_split.py:789-834. out_counts int64 [n_cols].
+ */
+int etm_popcount_cols(const uint64_t* bv, int64_t n_cols, int64_t n_words, int64_t ld, int64_t* out_counts,
+                      void* stream);
+
+/*
+ * Copy columns cols[0..n_f) of bv into out [n_f][out_ld] (words past n_words
+ * zeroed): the engine's private, padded copy of the frequent columns; the
+ * caller's array is only read (core/apriori.py:409-413). out_ld % 32 == 0.
+ */
+int etm_gather_cols(const uint64_t* bv, int64_t ld, const int32_t* cols, int32_t n_f, int64_t n_words,
+                    uint64_t* out, int64_t out_ld, void* stream);
+
+/*
+ * Deterministic Bernoulli bitvectors (workload generator; no reference
+ * counterpart): bit r of item i set when hash(seed, i, r) < thresholds[i].
+ */
+int etm_synth_bernoulli(const uint64_t* thresholds, int32_t n_items, int64_t n_rows, uint64_t seed,
+                        uint64_t* out_bv, int64_t ld, void* stream);
+
+/*
+ * Prefix groups of a level. Replaces build_k3plus_groups_from_flat
+ * (gpu/kernels/k3plus.py:243-301; rust_ext/src/core/groups.rs:59-248) and the
+ * prefix-run step of generate_candidates (core/cpu_miner.py:466-475).
+ * rows int32 [n][width] (width >= 1; width 1 = one group of every row).
+ * Outputs groups with >= 2 members: grp_first int64 [n], grp_size int32 [n],
+ * cand_off int64 [n+1] (exclusive prefix of C(m,2); cand_off[G] = total),
+ * counters int64 [2] = {G, total candidates}. ws: 2 * (n/4096 + 3) words.
+ */
+int etm_level_groups(const int32_t* rows, int64_t n, int32_t width, int64_t* grp_first, int32_t* grp_size,
+                     int64_t* cand_off, int64_t* counters, int64_t* ws, int64_t ws_words, void* stream);
+
+/*
+ * Subset test and count inference of the candidates of groups [g0, g1).
+ * Replaces _classify_candidate (gpu/kernels/_src/_subset_index.cu:139-178) and
+ * the CPU route's prune/infer steps (core/cpu_miner.py:490-494, 1119-1124).
+ * rows/counts/free_flags: the generating level (n_rows x width). mode:
+ * ETM_SUBSET_PRUNE (a missing prefix-dropping subset -> SKIP) | ETM_SUBSET_INFER
+ * (a non-free subset -> INFER with the minimum subset count, written to
+ * out_counts). out_cls uint8 and out_counts int32 are indexed by candidate
+ * minus cand_off[g0].
+ */
+int etm_classify(const int32_t* rows, int32_t width, int64_t n_rows, const int32_t* counts,
+                 const uint8_t* free_flags, const int64_t* grp_first, const int32_t* grp_size,
+                 const int64_t* cand_off, int64_t g0, int64_t g1, int32_t mode, uint8_t* out_cls,
+                 int32_t* out_counts, void* stream);
+
+/*
+ * Count the candidates of the listed groups by tile-pairs of 64 x 64
+ * suffixes (AND of the prefix columns per word, AND+popcount per pair).
+ * Replaces count_shared_tiled_dense (gpu/kernels/_src/shared_tiled.cu:96-246),
+ * count_group_pairs (group_pairs.cu:32-217) and, for K=2,
+ * count_pairs_k2_dense (pairs_k2_dense.cu:3-45).
+ * fbv [n_f][ld] (ld % 32 == 0, zero past n_words). work_groups int64 [n_work]
+ * group ids; work_off int64 [n_work+1] exclusive prefix of each listed
+ * group's tile-pairs T(T+1)/2, T = ceil(m/64). Counts go to
+ * out_counts[cand_off[g] - chunk_base + pair]. cls (nullable): candidates
+ * whose class is not ETM_CAND_COUNT are not written; tile-pairs without any
+ * are skipped. method: ETM_METHOD_POPCOUNT or ETM_METHOD_TENSOR.
+ */
+int etm_count_tiles(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                    const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
+                    const int64_t* work_groups, const int64_t* work_off, int64_t n_work, int64_t chunk_base,
+                    const uint8_t* cls, int32_t method, int32_t* out_counts, void* stream);
+
+/*
+ * Count candidates one warp each (AND of all k columns, popcount): the
+ * layout for small prefix groups. Replaces count_k3plus_dense
+ * (gpu/kernels/_src/k3plus_dense.cu:3-106). work_off int64 [n_work+1] is the
+ * exclusive prefix of C(m,2) over the listed groups.
+ */
+int etm_count_cands(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                    const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
+                    const int64_t* work_groups, const int64_t* work_off, int64_t n_work, int64_t chunk_base,
+                    const uint8_t* cls, int32_t* out_counts, void* stream);
+
+/*
+ * Survivors of a counted chunk (groups [g0, g1)), in candidate order, decoded
+ * into rows of width+1 columns. Replaces threshold_filter
+ * (gpu/kernels/filter.py:85-120), decode_k2_pairs_flat / decode_k3plus_flat
+ * (gpu/kernels/decode.py:9-73) and the level-end lexsort
+ * (gpu/row_split.py:1064-1067): the output is already lexicographic.
+ * A candidate survives when its count >= min_count and (cls NULL or its class
+ * is not SKIP). acc int64 [1] (device) is the running row total: rows are
+ * written at acc[0] + rank while that is < cap, and acc[0] grows by the
+ * survivors even past cap (the caller grows the output and repeats the call
+ * with acc reset). ws: n_cands/4096 + 3 words.
+ */
+int etm_level_compact(const int32_t* counts, const uint8_t* cls, int64_t n_cands, const int32_t* rows,
+                      int32_t width, const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
+                      int64_t g0, int64_t g1, int32_t min_count, int32_t* out_rows, int32_t* out_counts,
+                      int64_t cap, int64_t* acc, int64_t* ws, int64_t ws_words, void* stream);
+
+/*
+ * Free flags and subset presence of a new level (k = width + 1 columns)
+ * against the generating level prev (n_prev x width, with counts).
+ * Replaces the free-set tests (core/cpu_miner.py:943-945, 1139-1151;
+ * gpu/mining.py:81-139; rust_ext/src/core/groups.rs:250-312).
+ * out_free[t] = no (k-1)-subset of row t has its count; out_present[t] = every
+ * (k-1)-subset of row t is a row of prev. Either output may be NULL.
+ */
+int etm_level_subsets(const int32_t* new_rows, const int32_t* new_counts, int64_t n_new, int32_t width,
+                      const int32_t* prev_rows, const int32_t* prev_counts, int64_t n_prev, uint8_t* out_free,
+                      uint8_t* out_present, void* stream);
+
+/*
+ * Keep the rows whose keep[] flags are all set (the free-set prune,
+ * gpu/row_split.py:1075-1100), in order. keep_a / keep_b uint8 (keep_b
+ * nullable). acc and cap as in etm_level_compact. ws: n/4096 + 3 words.
+ */
+int etm_select_rows(const int32_t* rows, const int32_t* counts, const uint8_t* keep_a, const uint8_t* keep_b,
+                    int64_t n, int32_t width, int32_t* out_rows, int32_t* out_counts, uint8_t* out_flag_src,
+                    uint8_t* out_flag, int64_t cap, int64_t* acc, int64_t* ws, int64_t ws_words, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ETM_H */

@@ -1,0 +1,141 @@
+"""GPU parity: the engine through apriori() against the reference's golden results and the oracle.
+
+Every itemset and every count must be identical (bit-exact integer work).
+"""
+
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import miner
+from tests.conftest import case_input
+from tests.helpers import bitvecs_of, digest_pairs, table_of
+
+pytestmark = pytest.mark.gpu
+
+CASES = [c["name"] for c in json.loads((Path(__file__).parent / "golden" / "cases.json").read_text())["cases"]]
+
+
+@pytest.fixture(scope="module")
+def engines(pkg):
+    from importlib import import_module
+
+    eng = import_module(pkg.__name__ + ".engine")
+    return {
+        "batched": eng.Engine(form="batched"),
+        "plain": eng.Engine(form="plain"),
+        "tiny": eng.Engine(form="batched", chunk_cands=97, small_group=3),
+    }
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_transactions_match_golden(pkg, golden_cases, engines, name):
+    case = golden_cases[name]
+    indptr, items, n_rows = case_input(pkg, case)
+    got = pkg.apriori(table_of(indptr, items, n_rows), min_support=case["min_support"], max_length=case["max_length"],
+                      use_gpu=True, prune_equal_support=case["prune_equal_support"],
+                      use_generator_pruning=case["use_generator_pruning"], engine=engines["batched"],
+                      warn_complexity=False)
+    pairs = pkg.result_pairs(got, n_rows)
+    assert digest_pairs(pairs) == case["digest"], name
+    if "itemsets" in case:
+        want = sorted(((tuple(s), c) for s, c in case["itemsets"]), key=lambda t: (len(t[0]), t[0]))
+        assert pairs == want
+
+
+@pytest.mark.parametrize("form", ["plain", "tiny"])
+@pytest.mark.parametrize("name", ["implication_plain", "implication_prune", "implication_infer", "plain_small_plain",
+                                  "deep_sparse_small", "dense_k2_small", "word_tail_65"])
+def test_forms_match_golden(pkg, golden_cases, engines, name, form):
+    case = golden_cases[name]
+    indptr, items, n_rows = case_input(pkg, case)
+    got = pkg.apriori(table_of(indptr, items, n_rows), min_support=case["min_support"], max_length=case["max_length"],
+                      use_gpu=True, prune_equal_support=case["prune_equal_support"],
+                      use_generator_pruning=case["use_generator_pruning"], engine=engines[form],
+                      warn_complexity=False)
+    assert digest_pairs(pkg.result_pairs(got, n_rows)) == case["digest"]
+
+
+@pytest.mark.parametrize("prune,infer", [(False, False), (True, False), (False, True)])
+def test_bitvecs_route_matches_oracle(pkg, prune, infer):
+    import torch
+
+    syn = pkg.synthetic
+    t = syn.plain_small(n_rows=20_000, n_items=300, seed=5)
+    bv, col_to_item = bitvecs_of(t.indptr, t.items, t.n_rows)
+    dev = torch.from_numpy(bv.view(np.int64)).cuda().view(torch.uint64)
+    before = dev.clone()
+    got = pkg.apriori(bitvecs=(dev, col_to_item, t.n_rows), min_support=0.005, prune_equal_support=prune,
+                      use_generator_pruning=infer, warn_complexity=False)
+    ref = miner.mine_bitvecs(bv, t.n_rows, 0.005, prune_equal_support=prune, use_generator_pruning=infer)
+    items = np.array([col_to_item[c] for c in range(bv.shape[0])])
+    assert pkg.result_pairs(got, t.n_rows) == miner.canonical(ref.levels, items)
+    assert torch.equal(dev, before), "the caller's bitvectors must never be written"
+
+
+def test_dense_bernoulli_matches_oracle(pkg):
+    """A dense workload with wide prefix groups (several 64-suffix tiles per group)."""
+    import torch
+
+    syn = pkg.synthetic
+    p = syn.dense_k2_probs(300, seed=2) * 3
+    bv = syn.bernoulli_bitvecs(syn.bernoulli_thresholds(np.minimum(p, 0.9)), 6_000, seed=3)
+    dev = torch.from_numpy(bv.view(np.int64)).cuda().view(torch.uint64)
+    col_to_item = {c: c for c in range(bv.shape[0])}
+    got = pkg.apriori(bitvecs=(dev, col_to_item, 6_000), min_support=0.02, max_length=3, warn_complexity=False)
+    ref = miner.mine_bitvecs(bv, 6_000, 0.02, 3)
+    assert pkg.result_pairs(got, 6_000) == miner.canonical(ref.levels)
+
+
+def test_uint64_ids_near_2_63_are_kept(pkg):
+    """UInt64 item ids beyond Int64 stay UInt64 in the result (core/result.py:30-54)."""
+    base = (1 << 63) - 3
+    rows = [[base, base + 1, base + 5], [base, base + 5], [base + 1, base + 5], [base, base + 1, base + 5]]
+    got = pkg.apriori(rows, min_support=0.5, use_gpu=True, warn_complexity=False)
+    pairs = dict(pkg.result_pairs(got, 4))
+    assert pairs[(base, base + 5)] == 3
+    assert pairs[(base, base + 1, base + 5)] == 2
+    if isinstance(got, pkg.ItemsetFrame):
+        assert got.item_dtype == np.uint64
+
+
+def test_edge_inputs(pkg):
+    assert len(pkg.result_pairs(pkg.apriori([], min_support=0.5, use_gpu=True), 1)) == 0
+    one = [[4, 2, 2, 9]]
+    pairs = pkg.result_pairs(pkg.apriori(one, min_support=1.0, use_gpu=True), 1)
+    assert pairs == [((2,), 1), ((4,), 1), ((9,), 1), ((2, 4), 1), ((2, 9), 1), ((4, 9), 1), ((2, 4, 9), 1)]
+    got = pkg.apriori(one, min_support=0.0, max_length=1, use_gpu=True)
+    assert pkg.result_pairs(got, 1) == [((2,), 1), ((4,), 1), ((9,), 1)]
+    # An item in every row is not free: the free-set prune drops it and everything above it.
+    rows = [[1, 2], [1, 3], [1, 2, 3], [1]]
+    got = pkg.apriori(rows, min_support=0.25, use_gpu=True, prune_equal_support=True)
+    assert pkg.result_pairs(got, 4) == [((2,), 2), ((3,), 2), ((2, 3), 1)]
+
+
+def test_validation_errors(pkg):
+    import torch
+
+    dev = torch.zeros((3, 2), dtype=torch.uint64, device="cuda")
+    with pytest.raises(ValueError, match="ceil"):
+        pkg.apriori(bitvecs=(dev, {0: 1, 1: 2, 2: 3}, 200))
+    with pytest.raises(ValueError, match="col_to_item"):
+        pkg.apriori(bitvecs=(dev, {0: 1}, 100))
+    with pytest.raises(ValueError, match="uint64"):
+        pkg.apriori(bitvecs=(dev.view(torch.int64), {0: 1, 1: 2, 2: 3}, 100))
+    with pytest.raises(ValueError, match="both"):
+        pkg.apriori([[1]], bitvecs=(dev, {0: 1, 1: 2, 2: 3}, 100))
+    with pytest.raises(ValueError, match="n_transactions"):
+        pkg.apriori(bitvecs=(torch.zeros((1, 1), dtype=torch.uint64, device="cuda"), {0: 1}, 1 << 31))
+
+
+def test_level_callback_and_profile(pkg):
+    calls = []
+    df, session = pkg.apriori([[1, 2, 3], [2, 3, 4], [1, 3, 5], [2, 3]], min_support=0.25, use_gpu=True,
+                              level_callback=lambda *a: calls.append(a), profile=True)
+    assert [c[0] for c in calls] == [1, 2, 3]
+    assert [c[2] for c in calls] == [5, 7, 3]
+    assert [p.name for p in session.phases] == ["k1", "k2", "k3"]

@@ -1,0 +1,237 @@
+"""Kernel-level GPU checks through the C ABI: each entry point against a host restatement."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import miner
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lib(pkg):
+    return pkg.load_library()
+
+
+def _stream():
+    import torch
+
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _dev(a):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.mark.parametrize("n_rows", [1, 63, 64, 65, 1000, 100_003])
+def test_build_bitvecs_is_byte_identical(pkg, lib, n_rows):
+    import torch
+
+    rng = np.random.default_rng(n_rows)
+    n_items = 37
+    lens = rng.integers(0, 12, n_rows)
+    indptr = np.zeros(n_rows + 1, np.int64)
+    np.cumsum(lens, out=indptr[1:])
+    rows = [np.sort(rng.choice(n_items, size=l, replace=False)) for l in lens]
+    ids = np.concatenate(rows).astype(np.int32) if rows else np.zeros(0, np.int32)
+    want = miner.bitvecs_from_csr(indptr, ids, n_items, n_rows)
+    ld = (n_rows + 63) // 64
+    out = torch.full((n_items, ld), -1, dtype=torch.int64, device="cuda")
+    d_ptr, d_ids = _dev(indptr), _dev(ids if len(ids) else np.zeros(1, np.int32))
+    st = lib.etm_build_bitvecs(d_ptr.data_ptr(), d_ids.data_ptr(), len(ids), None, 0, n_rows, n_items, ld,
+                               out.data_ptr(), _stream())
+    assert st == 0, lib.etm_last_error()
+    assert np.array_equal(out.cpu().numpy().view(np.uint64), want)
+
+
+def test_build_bitvecs_with_lut(pkg, lib):
+    """ids go through an id -> column table; -1 and out-of-range ids are dropped (csr_to_bitvec.cu:46-73)."""
+    import torch
+
+    indptr = np.array([0, 3, 5, 6], np.int64)
+    ids = np.array([7, 2, 9, 2, 100, 7], np.int32)
+    lut = np.full(10, -1, np.int32)
+    lut[2], lut[7] = 0, 1
+    out = torch.zeros((2, 1), dtype=torch.int64, device="cuda")
+    d = [_dev(indptr), _dev(ids), _dev(lut)]
+    st = lib.etm_build_bitvecs(d[0].data_ptr(), d[1].data_ptr(), len(ids), d[2].data_ptr(), 10, 3, 2, 1,
+                               out.data_ptr(), _stream())
+    assert st == 0
+    assert out.cpu().numpy().tolist() == [[0b011], [0b101]]
+
+
+def test_popcount_and_gather(pkg, lib):
+    import torch
+
+    rng = np.random.default_rng(1)
+    bv = rng.integers(0, 2**63, size=(50, 1001), dtype=np.int64).view(np.uint64)
+    d = _dev(bv.view(np.int64))
+    out = torch.empty(50, dtype=torch.int64, device="cuda")
+    assert lib.etm_popcount_cols(d.data_ptr(), 50, 1000, 1001, out.data_ptr(), _stream()) == 0
+    assert np.array_equal(out.cpu().numpy(), np.bitwise_count(bv[:, :1000]).sum(axis=1))
+    cols = np.array([3, 0, 49], np.int32)
+    g = torch.full((3, 1024), -1, dtype=torch.int64, device="cuda")
+    d_cols = _dev(cols)
+    assert lib.etm_gather_cols(d.data_ptr(), 1001, d_cols.data_ptr(), 3, 1000, g.data_ptr(), 1024, _stream()) == 0
+    got = g.cpu().numpy().view(np.uint64)
+    assert np.array_equal(got[:, :1000], bv[cols, :1000]) and not got[:, 1000:].any()
+
+
+def test_synth_bernoulli_matches_host_twin(pkg, lib):
+    import torch
+
+    syn = pkg.synthetic
+    thr = syn.bernoulli_thresholds(syn.dense_k2_probs(40, seed=4))
+    n_rows = 3_000
+    want = syn.bernoulli_bitvecs(thr, n_rows, seed=99)
+    ld = (n_rows + 63) // 64
+    out = torch.empty((40, ld), dtype=torch.int64, device="cuda")
+    d_thr = _dev(thr.view(np.int64))
+    assert lib.etm_synth_bernoulli(d_thr.data_ptr(), 40, n_rows, 99, out.data_ptr(), ld, _stream()) == 0
+    assert np.array_equal(out.cpu().numpy().view(np.uint64), want)
+
+
+def _host_groups(rows):
+    n, w = rows.shape
+    if n == 0:
+        return []
+    key = [tuple(r[: w - 1]) for r in rows]
+    out, s = [], 0
+    for t in range(1, n + 1):
+        if t == n or key[t] != key[s]:
+            if t - s >= 2:
+                out.append((s, t - s))
+            s = t
+    return out
+
+
+@pytest.mark.parametrize("width", [1, 2, 3])
+def test_level_groups(pkg, lib, width):
+    import torch
+
+    rng = np.random.default_rng(width)
+    rows = np.unique(rng.integers(0, 12, size=(400, width)), axis=0).astype(np.int32)
+    rows = rows[np.all(np.diff(rows, axis=1) > 0, axis=1)] if width > 1 else rows
+    n = len(rows)
+    want = _host_groups(rows)
+    gf = torch.empty(n, dtype=torch.int64, device="cuda")
+    gs = torch.empty(n, dtype=torch.int32, device="cuda")
+    co = torch.empty(n + 1, dtype=torch.int64, device="cuda")
+    cnt = torch.empty(2, dtype=torch.int64, device="cuda")
+    ws = torch.empty(3 + n // 4096 + 3, dtype=torch.int64, device="cuda")
+    d_rows = _dev(rows)
+    assert lib.etm_level_groups(d_rows.data_ptr(), n, width, gf.data_ptr(), gs.data_ptr(), co.data_ptr(),
+                                cnt.data_ptr(), ws.data_ptr(), ws.numel(), _stream()) == 0, lib.etm_last_error()
+    G, total = cnt.cpu().tolist()
+    assert G == len(want)
+    assert list(zip(gf[:G].cpu().tolist(), gs[:G].cpu().tolist())) == want
+    pairs = [m * (m - 1) // 2 for _, m in want]
+    assert co[: G + 1].cpu().tolist() == [0] + np.cumsum(pairs).tolist()
+    assert total == sum(pairs)
+
+
+def test_classify_labels(pkg, lib):
+    """SKIP / INFER labels on the implication dataset against a brute-force host labelling."""
+    import torch
+
+    from tests.golden.make_golden import _implication
+
+    rows_list = _implication()
+    indptr = np.r_[0, np.cumsum([len(r) for r in rows_list])].astype(np.int64)
+    items = np.concatenate([np.array(r) for r in rows_list]).astype(np.int64)
+    n_rows = len(rows_list)
+    res, col_items = miner.mine_transactions(indptr, items, n_rows, 0.01, 3, use_generator_pruning=True)
+    l2_sets, l2_counts = res.levels[1]
+    csr = miner.transaction_csr(indptr, items, n_rows, 0.01)
+    bv = miner.bitvecs_from_csr(csr.indptr, csr.cols, csr.n_cols, n_rows)
+    idx1 = miner.LevelIndex(res.levels[0][0], csr.n_cols)
+    pos = miner.subset_positions(idx1, l2_sets)
+    free2 = ~np.any(res.levels[0][1][pos] == l2_counts[:, None], axis=1)
+    groups = _host_groups(l2_sets)
+    cands, labels, inferred = [], [], []
+    index = {tuple(r): t for t, r in enumerate(l2_sets.tolist())}
+    for first, m in groups:
+        for i in range(m):
+            for j in range(i + 1, m):
+                c = list(l2_sets[first + i]) + [l2_sets[first + j][1]]
+                cands.append(c)
+                subs = [tuple(x for x in c if x != y) for y in c]
+                found = [index.get(s) for s in subs]
+                if found[0] is None:
+                    labels.append(1)
+                    inferred.append(0)
+                elif not all(free2[f] for f in found):
+                    labels.append(2)
+                    inferred.append(min(l2_counts[f] for f in found))
+                else:
+                    labels.append(0)
+                    inferred.append(0)
+    n = len(l2_sets)
+    gf = torch.tensor([f for f, _ in groups], dtype=torch.int64, device="cuda")
+    gs = torch.tensor([m for _, m in groups], dtype=torch.int32, device="cuda")
+    co = torch.tensor([0] + np.cumsum([m * (m - 1) // 2 for _, m in groups]).tolist(), dtype=torch.int64, device="cuda")
+    cls = torch.empty(len(cands), dtype=torch.uint8, device="cuda")
+    cnt = torch.zeros(len(cands), dtype=torch.int32, device="cuda")
+    d = [_dev(l2_sets.astype(np.int32)), _dev(l2_counts.astype(np.int32)), _dev(free2.astype(np.uint8))]
+    st = lib.etm_classify(d[0].data_ptr(), 2, n, d[1].data_ptr(), d[2].data_ptr(), gf.data_ptr(), gs.data_ptr(),
+                          co.data_ptr(), 0, len(groups), 3, cls.data_ptr(), cnt.data_ptr(), _stream())
+    assert st == 0
+    got = cls.cpu().numpy()
+    assert got.tolist() == labels
+    inf = np.array(labels) == 2
+    assert inf.any() and (np.array(labels) == 1).any()
+    assert np.array_equal(cnt.cpu().numpy()[inf], np.array(inferred)[inf])
+    # Inferred counts are exact: they equal the counted support.
+    true = miner.count_itemsets(np.array(cands, dtype=np.int32)[inf], bv)
+    assert np.array_equal(true, np.array(inferred)[inf])
+
+
+@pytest.mark.parametrize("method", ["popcount"])
+def test_pair_counts_all_pairs(pkg, method):
+    """K=2 as one group: every pair count equals the host AND+popcount, word tails 1/31/32/33/65."""
+    import torch
+
+    from importlib import import_module
+
+    eng = import_module(pkg.__name__ + ".engine").Engine(method=method)
+    for n_words in (1, 31, 32, 33, 65):
+        rng = np.random.default_rng(n_words)
+        n_rows = n_words * 64 - 5
+        n_f = 150
+        bv = rng.integers(0, 2**63, size=(n_f, n_words), dtype=np.int64).view(np.uint64)
+        bv[:, -1] &= np.uint64((1 << 59) - 1)
+        dev = torch.from_numpy(bv.view(np.int64)).cuda()
+        fbv, ldp = eng.gather(dev.data_ptr(), n_words, np.arange(n_f), n_words)
+        gen = import_module(pkg.__name__ + ".engine").Level(
+            torch.arange(n_f, dtype=torch.int32, device="cuda")[:, None].contiguous(),
+            torch.ones(n_f, dtype=torch.int32, device="cuda"))
+        new, _ = eng.count_level(gen, fbv, ldp, n_words, 1, False, False)
+        ii, jj = np.triu_indices(n_f, 1)
+        want = np.bitwise_count(bv[ii] & bv[jj]).sum(axis=1)
+        keep = want >= 1
+        assert np.array_equal(new.rows.cpu().numpy(), np.stack([ii, jj], 1)[keep])
+        assert np.array_equal(new.counts.cpu().numpy(), want[keep])
+        del n_rows
+
+
+def test_compaction_overflow_regrows(pkg):
+    """A survivor count beyond the first output capacity regrows and repeats the chunk."""
+    import torch
+
+    from importlib import import_module
+
+    engm = import_module(pkg.__name__ + ".engine")
+    eng = engm.Engine(chunk_cands=1000)
+    rng = np.random.default_rng(7)
+    n_f, n_words = 700, 4
+    bv = rng.integers(0, 2**63, size=(n_f, n_words), dtype=np.int64)
+    dev = torch.from_numpy(bv).cuda()
+    fbv, ldp = eng.gather(dev.data_ptr(), n_words, np.arange(n_f), n_words)
+    gen = engm.Level(torch.arange(n_f, dtype=torch.int32, device="cuda")[:, None].contiguous(),
+                     torch.ones(n_f, dtype=torch.int32, device="cuda"))
+    new, stats = eng.count_level(gen, fbv, ldp, n_words, 1, False, False)
+    assert new.n == n_f * (n_f - 1) // 2 and stats.n_chunks > 100
