@@ -42,6 +42,7 @@ import numpy as np  # noqa: E402
 
 WORKLOADS = {
     "dense_k2": dict(n_items=4096, n_rows=2_000_000, min_support=0.002, max_length=3, seed=0, hash_seed=12345),
+    "dense_k2_mid": dict(n_items=2048, n_rows=1_000_000, min_support=0.002, max_length=3, seed=0, hash_seed=12345),
     "dense_k2_small": dict(n_items=1024, n_rows=500_000, min_support=0.002, max_length=3, seed=0, hash_seed=12345),
 }
 

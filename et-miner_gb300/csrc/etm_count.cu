@@ -27,14 +27,20 @@ struct TileShared {
     uint64_t a[TT * STRIDE];
     uint64_t b[TT * STRIDE];
     uint64_t pre[WCH];
-    int32_t sa[TT];
-    int32_t sb[TT];
+    int64_t oa[TT];  // word offset of each A / B suffix row in `src`, -1 past the group
+    int64_t ob[TT];
     int32_t pref[MAXP + 1];
-    int flag;
 };
 
+// Tile-pair counting over one of two sources:
+//   PROJ = false: the padded frequent columns fbv [n_f][ld]; a group's suffix i is
+//                 column rows[first+i][width-1]; the prefix columns are ANDed in per word.
+//   PROJ = true:  compacted suffix bitvectors: work entry wi's member i is at
+//                 src + cbase[wi] + i * cld[wi], cwords[wi] words long, prefix already applied.
+template <bool PROJ>
 __global__ void __launch_bounds__(TILE_THREADS) count_tiles_popc_kernel(
-    const uint64_t* __restrict__ fbv, int64_t ld, int64_t n_words, const int32_t* __restrict__ rows, int width,
+    const uint64_t* __restrict__ src, int64_t ld, int64_t n_words, const int64_t* __restrict__ cbase,
+    const int64_t* __restrict__ cwords, const int64_t* __restrict__ cld, const int32_t* __restrict__ rows, int width,
     const int64_t* __restrict__ grp_first, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
     const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
     const uint8_t* __restrict__ cls, int32_t* __restrict__ out) {
@@ -42,8 +48,7 @@ __global__ void __launch_bounds__(TILE_THREADS) count_tiles_popc_kernel(
     const int tid = threadIdx.x;
     const int ty = tid >> 4, tx = tid & 15;
     const int64_t total = work_off[n_work];
-    const int plen = width - 1;
-    const int64_t n_slabs = ceil_div<int64_t>(n_words, WCH);
+    const int plen = PROJ ? 0 : width - 1;
 
     for (int64_t tp = blockIdx.x; tp < total; tp += gridDim.x) {
         const int64_t wi = upper_find(work_off, n_work, tp);
@@ -53,13 +58,21 @@ __global__ void __launch_bounds__(TILE_THREADS) count_tiles_popc_kernel(
         int64_t ti, tj1;
         tri_decode(tp - work_off[wi], nt + 1, &ti, &tj1);
         const int64_t tj = tj1 - 1;
-        const int64_t first = grp_first[g];
+        const int64_t first = PROJ ? 0 : grp_first[g];  // the projected source needs no rows
         const int64_t cb = cand_off[g] - chunk_base;
+        const int64_t words = PROJ ? cwords[wi] : n_words;
+        const int64_t n_slabs = ceil_div<int64_t>(words, WCH);
 
         if (tid < TT) {
             const int64_t ia = ti * TT + tid, ib = tj * TT + tid;
-            sh.sa[tid] = ia < m ? rows[(first + ia) * width + plen] : -1;
-            sh.sb[tid] = ib < m ? rows[(first + ib) * width + plen] : -1;
+            if (PROJ) {
+                const int64_t b0 = cbase[wi], st = cld[wi];
+                sh.oa[tid] = ia < m ? b0 + ia * st : -1;
+                sh.ob[tid] = ib < m ? b0 + ib * st : -1;
+            } else {
+                sh.oa[tid] = ia < m ? (int64_t)rows[(first + ia) * width + width - 1] * ld : -1;
+                sh.ob[tid] = ib < m ? (int64_t)rows[(first + ib) * width + width - 1] * ld : -1;
+            }
         }
         if (tid < plen) sh.pref[tid] = rows[first * width + tid];
 
@@ -87,25 +100,31 @@ __global__ void __launch_bounds__(TILE_THREADS) count_tiles_popc_kernel(
 
         for (int64_t s = 0; s < n_slabs; s++) {
             const int64_t w0 = s * WCH;
-            if (tid < WCH) {
-                uint64_t p = ~0ULL;
-                for (int q = 0; q < plen; q++) p &= __ldg(fbv + (int64_t)sh.pref[q] * ld + w0 + tid);
-                sh.pre[tid] = p;
+            if (!PROJ) {
+                if (tid < WCH) {
+                    uint64_t p = ~0ULL;
+                    for (int q = 0; q < plen; q++) p &= __ldg(src + (int64_t)sh.pref[q] * ld + w0 + tid);
+                    sh.pre[tid] = p;
+                }
+                __syncthreads();
+                const int live = tid < WCH ? (sh.pre[tid] != 0ULL) : 0;
+                if (!__syncthreads_or(live)) continue;
             }
-            __syncthreads();
-            const int live = tid < WCH ? (sh.pre[tid] != 0ULL) : 0;
-            if (!__syncthreads_or(live)) continue;
             // Stage A (masked by the prefix) and B: 64 rows x 16 vectors each.
 #pragma unroll
             for (int q = 0; q < (TT * WCH / 2) / TILE_THREADS; q++) {
                 const int idx = q * TILE_THREADS + tid;
                 const int r = idx >> 4, v = idx & 15;
-                const int ca = sh.sa[r], cbb = sh.sb[r];
+                const int64_t oa = sh.oa[r], ob = sh.ob[r];
                 ulonglong2 xa = make_ulonglong2(0, 0), xb = make_ulonglong2(0, 0);
-                if (ca >= 0) xa = __ldg(reinterpret_cast<const ulonglong2*>(fbv + (int64_t)ca * ld + w0) + v);
-                if (cbb >= 0) xb = __ldg(reinterpret_cast<const ulonglong2*>(fbv + (int64_t)cbb * ld + w0) + v);
-                sh.a[r * STRIDE + 2 * v] = xa.x & sh.pre[2 * v];
-                sh.a[r * STRIDE + 2 * v + 1] = xa.y & sh.pre[2 * v + 1];
+                if (oa >= 0) xa = __ldg(reinterpret_cast<const ulonglong2*>(src + oa + w0) + v);
+                if (ob >= 0) xb = __ldg(reinterpret_cast<const ulonglong2*>(src + ob + w0) + v);
+                if (!PROJ) {
+                    xa.x &= sh.pre[2 * v];
+                    xa.y &= sh.pre[2 * v + 1];
+                }
+                sh.a[r * STRIDE + 2 * v] = xa.x;
+                sh.a[r * STRIDE + 2 * v + 1] = xa.y;
                 sh.b[r * STRIDE + 2 * v] = xb.x;
                 sh.b[r * STRIDE + 2 * v + 1] = xb.y;
             }
@@ -196,10 +215,23 @@ int count_tiles_popcount(const uint64_t* fbv, int64_t ld, int64_t n_words, const
                          const int64_t* work_groups, const int64_t* work_off, int64_t n_work, int64_t chunk_base,
                          const uint8_t* cls, int32_t* out, int64_t n_tiles_hint, cudaStream_t s) {
     const int64_t cap = (int64_t)max(1, sm_count()) * 6;
-    const int grid = (int)max64(1, min(cap, n_tiles_hint > 0 ? n_tiles_hint : cap));
-    count_tiles_popc_kernel<<<grid, TILE_THREADS, 0, s>>>(fbv, ld, n_words, rows, width, grp_first, grp_size, cand_off,
-                                                          work_groups, work_off, n_work, chunk_base, cls, out);
+    const int grid = (int)max64(1, min64(cap, n_tiles_hint > 0 ? n_tiles_hint : cap));
+    count_tiles_popc_kernel<false><<<grid, TILE_THREADS, 0, s>>>(fbv, ld, n_words, nullptr, nullptr, nullptr, rows,
+                                                                 width, grp_first, grp_size, cand_off, work_groups,
+                                                                 work_off, n_work, chunk_base, cls, out);
     ETM_LAUNCHED("count_tiles_popc");
+    return ETM_OK;
+}
+
+int count_tiles_proj_popcount(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
+                              const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
+                              const int64_t* work_off, int64_t n_work, int64_t chunk_base, const uint8_t* cls,
+                              int32_t* out, cudaStream_t s) {
+    const int grid = max(1, sm_count()) * 6;
+    count_tiles_popc_kernel<true><<<grid, TILE_THREADS, 0, s>>>(cbuf, 0, 0, cbase, cwords, cld, nullptr, 1, nullptr,
+                                                                grp_size, cand_off, work_groups, work_off, n_work,
+                                                                chunk_base, cls, out);
+    ETM_LAUNCHED("count_tiles_proj_popc");
     return ETM_OK;
 }
 

@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_partials_kernel(int64_t n, 
 
 // One block: exclusive scan of partial[0..nb) in place; base = *acc (or 0);
 // partial[nb] = base (kept for phase 3), *acc = base + sum.
-__global__ void __launch_bounds__(1024) scan_offsets_kernel(int64_t nb, int64_t* partial, int64_t* acc) {
+static __global__ void __launch_bounds__(1024) scan_offsets_kernel(int64_t nb, int64_t* partial, int64_t* acc) {
     __shared__ int64_t carry;
     if (threadIdx.x == 0) carry = acc ? *acc : 0;
     __syncthreads();

@@ -42,6 +42,11 @@ SMALL_GROUP = 16
 TILE = 64
 #: Candidates per chunk (int32 count + uint8 class each): bounds the level's dense scratch.
 CHUNK_CANDS = 1 << 27
+#: A group of more than SMALL_GROUP members is counted on its prefix's rows only when the prefix
+#: holds less than this fraction of the transactions.
+PROJ_DENSITY = 0.5
+#: Device bytes of projected suffix words (and row lists) per chunk.
+PROJ_BYTES = 4 << 30
 #: Counting method for tile-pairs: "popcount" or "tensor".
 DEFAULT_METHOD = "popcount"
 
@@ -179,7 +184,8 @@ class Engine:
     """One device's mining state: the library, scratch buffers and the counting choices."""
 
     def __init__(self, device: torch.device | int | None = None, *, method: str = DEFAULT_METHOD,
-                 form: str = "batched", chunk_cands: int = CHUNK_CANDS, small_group: int = SMALL_GROUP):
+                 form: str = "batched", chunk_cands: int = CHUNK_CANDS, small_group: int = SMALL_GROUP,
+                 project: bool = True, proj_density: float = PROJ_DENSITY, proj_bytes: int = PROJ_BYTES):
         if not torch.cuda.is_available():
             raise RuntimeError("the GB300 engine needs a CUDA device; there is no CPU fallback")
         self.lib = load_library()
@@ -193,6 +199,9 @@ class Engine:
         self.form = form
         self.chunk_cands = int(chunk_cands)
         self.small_group = int(small_group)
+        self.project = bool(project)
+        self.proj_density = float(proj_density)
+        self.proj_bytes = int(proj_bytes)
         self.scratch = _Scratch(self.device)
         self.launches = 0
         #: When set, every counting / compaction launch is bracketed by CUDA events on its stream.
@@ -264,11 +273,71 @@ class Engine:
         both = torch.from_numpy(np.concatenate([ids.astype(np.int64), off])).to(self.device, non_blocking=False)
         return both[: len(ids)], both[len(ids):]
 
+    def prefix_counts(self, fbv, ldp: int, n_words: int, gen: Level, grp_first, ids: np.ndarray) -> np.ndarray:
+        """Rows holding each listed group's prefix (popcount of the AND of its prefix columns)."""
+        wg = torch.from_numpy(ids.astype(np.int64)).to(self.device)
+        out = self.scratch.get("prefix_counts", len(ids), torch.int64)
+        st = self._launch("prefix_counts", len(ids) * (gen.k - 1) * n_words * 8, lambda: self.lib.etm_prefix_counts(
+            _p(fbv), ldp, n_words, _p(gen.rows), gen.k, _p(grp_first), _p(wg), len(ids), _p(out), _stream()))
+        check(st, "etm_prefix_counts")
+        self.launches += 1
+        return out.cpu().numpy().copy()
+
+    def _count_projected(self, fbv, ldp, n_words, gen, grp_first, grp_size, cand_off, gids, sizes, pcnt, base, cls,
+                         counts, method):
+        """Row lists, projected suffix words and tile-pair counts of the listed groups (one launch each)."""
+        width = gen.k
+        m = sizes[gids]
+        cnt = pcnt[gids]
+        cw = (cnt + 63) // 64
+        cl = np.maximum(32, (cw + 31) // 32 * 32)
+        row_off = np.zeros(len(gids) + 1, np.int64)
+        np.cumsum(cnt, out=row_off[1:])
+        mem_off = np.zeros(len(gids) + 1, np.int64)
+        np.cumsum(m, out=mem_off[1:])
+        cb = np.zeros(len(gids) + 1, np.int64)
+        np.cumsum(m * cl, out=cb[1:])
+        nt = (m + TILE - 1) // TILE
+        toff = np.zeros(len(gids) + 1, np.int64)
+        np.cumsum(nt * (nt + 1) // 2, out=toff[1:])
+        n = len(gids)
+        host = np.concatenate([gids.astype(np.int64), toff, row_off, mem_off, cb[:-1], cw, cl])
+        d = torch.from_numpy(host).to(self.device)
+        wg, wo = d[:n], d[n:2 * n + 1]
+        ro, mo = d[2 * n + 1:3 * n + 2], d[3 * n + 2:4 * n + 3]
+        cbase, cwords, cld = d[4 * n + 3:5 * n + 3], d[5 * n + 3:6 * n + 3], d[6 * n + 3:7 * n + 3]
+        rowidx = self.scratch.get("proj_rows", int(row_off[-1]), torch.int32)
+        cbuf = self.scratch.get("proj_cbuf", int(cb[-1]), torch.int64)
+        st = self._launch("prefix_rows", int(n * (width - 1) * n_words * 8 + row_off[-1] * 4),
+                          lambda: self.lib.etm_prefix_rows(_p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first),
+                                                           _p(wg), n, _p(ro), _p(rowidx), _stream()))
+        check(st, "etm_prefix_rows")
+        st = self._launch("project", int((m * cnt).sum() * 4 // 32 + (m * cl).sum() * 8 + (m * cnt).sum() // 8),
+                          lambda: self.lib.etm_project(_p(fbv), ldp, _p(gen.rows), width, _p(grp_first), _p(wg),
+                                                       _p(mo), n, _p(ro), _p(rowidx), _p(cbase), _p(cld), _p(cbuf),
+                                                       _stream()))
+        check(st, "etm_project")
+        st = self._launch("count_tiles_proj", int((m * cw).sum() * 8),
+                          lambda: self.lib.etm_count_tiles_proj(_p(cbuf), _p(cbase), _p(cwords), _p(cld),
+                                                                _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, base,
+                                                                _p(cls), method, _p(counts), _stream()))
+        check(st, "etm_count_tiles_proj")
+        self.launches += 3
+
     def count_level(self, gen: Level, fbv: torch.Tensor, ldp: int, n_words: int, mc: int,
-                    infer: bool, prune: bool) -> tuple[Level, LevelStats]:
-        """Count every candidate of the level generated by ``gen``; returns the survivors (k = gen.k + 1)."""
+                    infer: bool, prune: bool, n_rows: int | None = None) -> tuple[Level, LevelStats]:
+        """Count every candidate of the level generated by ``gen``; returns the survivors (k = gen.k + 1).
+
+        Groups with at most ``small_group`` members are counted one warp per
+        candidate; larger groups by 64 x 64 tile-pairs, on the prefix's rows
+        only (projected) when the prefix holds less than ``proj_density`` of the
+        transactions, else on the full bitvectors with the prefix ANDed in.
+        Chunks of whole groups bound the dense count scratch (``chunk_cands``)
+        and the projection scratch (``proj_bytes``).
+        """
         t0 = time.perf_counter()
         width = gen.k
+        n_rows = n_words * 64 if n_rows is None else n_rows
         G, total, grp_first, grp_size, cand_off = self.groups(gen)
         stats = LevelStats(width + 1, total, 0, 0.0, G)
         out_rows = torch.empty((0, width + 1), dtype=torch.int32, device=self.device)
@@ -281,6 +350,17 @@ class Engine:
         # The subset test has prefix subsets to look up only from K=3 on.
         classify = (infer or prune) and width >= 2
         mode = (1 if prune or infer else 0) | (2 if infer else 0)
+        big = sizes > self.small_group
+        pcnt = np.zeros(G, np.int64)
+        proj = np.zeros(G, bool)
+        if self.project and width >= 2 and big.any():
+            ids_big = np.flatnonzero(big)
+            pcnt[ids_big] = self.prefix_counts(fbv, ldp, n_words, gen, grp_first, ids_big)
+            proj = big & (pcnt < self.proj_density * n_rows)
+        pwords = np.maximum(32, ((pcnt + 63) // 64 + 31) // 32 * 32)
+        pbytes = np.where(proj, sizes * pwords * 8 + pcnt * 4, 0)
+        pcum = np.zeros(G + 1, np.int64)
+        np.cumsum(pbytes, out=pcum[1:])
         cap = int(min(total, max(1 << 16, 2 * gen.n)))
         out_rows = torch.empty((cap, width + 1), dtype=torch.int32, device=self.device)
         out_counts = torch.empty(cap, dtype=torch.int32, device=self.device)
@@ -290,25 +370,32 @@ class Engine:
         method = 1 if self.method == "tensor" else 0
         g0 = 0
         while g0 < G:
-            # Chunk: whole groups whose candidates fit the budget (at least one group).
-            limit = offs[g0] + max(self.chunk_cands, int(offs[g0 + 1] - offs[g0]))
-            g1 = int(np.searchsorted(offs, limit, side="right")) - 1
-            g1 = max(g1, g0 + 1)
+            # Chunk: whole groups within both budgets (at least one group).
+            g1c = int(np.searchsorted(offs, offs[g0] + self.chunk_cands, side="right")) - 1
+            g1p = int(np.searchsorted(pcum, pcum[g0] + self.proj_bytes, side="right")) - 1
+            g1 = max(min(g1c, g1p), g0 + 1)
             base = int(offs[g0])
             n_c = int(offs[g1] - base)
             counts = self.scratch.get("chunk_counts", n_c, torch.int32)
             cls = self.scratch.get("chunk_cls", n_c, torch.uint8) if classify else None
             if classify:
-                check(self.lib.etm_classify(_p(gen.rows), width, gen.n, _p(gen.counts), _p(gen.free),
-                                            _p(grp_first), _p(grp_size), _p(cand_off), g0, g1, mode, _p(cls),
-                                            _p(counts), _stream()), "etm_classify")
+                check(self._launch("classify", n_c * 5, lambda: self.lib.etm_classify(
+                    _p(gen.rows), width, gen.n, _p(gen.counts), _p(gen.free), _p(grp_first), _p(grp_size),
+                    _p(cand_off), g0, g1, mode, _p(cls), _p(counts), _stream())), "etm_classify")
                 self.launches += 1
             m = sizes[g0:g1]
             ids = np.arange(g0, g1, dtype=np.int64)
             small = m <= self.small_group
-            for kind, sel in (("cands", small), ("tiles", ~small)):
+            pr = proj[g0:g1]
+            for kind, sel in (("cands", small), ("tiles", ~small & ~pr), ("proj", pr)):
                 gids = ids[sel]
                 if len(gids) == 0:
+                    continue
+                if kind == "proj":
+                    groups = [gids] if self.form == "batched" else [gids[q:q + 1] for q in range(len(gids))]
+                    for bg in groups:
+                        self._count_projected(fbv, ldp, n_words, gen, grp_first, grp_size, cand_off, bg, sizes, pcnt,
+                                              base, cls, counts, method)
                     continue
                 if kind == "cands":
                     w = m[sel] * (m[sel] - 1) // 2
@@ -421,7 +508,7 @@ class Engine:
         k = 2
         while k <= max_k and gen.n >= k:
             t_level = time.perf_counter()
-            new, stats = self.count_level(gen, fbv, ldp, n_words, mc, infer, prune)
+            new, stats = self.count_level(gen, fbv, ldp, n_words, mc, infer, prune, n_rows)
             new = self.finish_level(new, gen, track_free, prune)
             stats.n_frequent = new.n
             stats.ms = (time.perf_counter() - t_level) * 1e3
@@ -438,5 +525,6 @@ class Engine:
 
 def mine(bitvecs, n_rows: int, min_support: float, max_length: int | None = None, **kw) -> MineOutput:
     """Mine device bitvectors [n_cols, ceil(N/64)] with a fresh ``Engine`` (see ``Engine.mine``)."""
-    engine_kw = {k: kw.pop(k) for k in ("method", "form", "chunk_cands", "small_group", "device") if k in kw}
+    engine_kw = {k: kw.pop(k) for k in ("method", "form", "chunk_cands", "small_group", "device", "project",
+                                        "proj_density", "proj_bytes") if k in kw}
     return Engine(**engine_kw).mine(bitvecs, n_rows, min_support, max_length, **kw)

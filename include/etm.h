@@ -150,6 +150,35 @@ int etm_count_cands(const uint64_t* fbv, int64_t ld, int64_t n_words, const int3
                     const uint8_t* cls, int32_t* out_counts, void* stream);
 
 /*
+ * Prefix projection (the reference's projection counting of wide groups,
+ * core/cpu_miner.py:720-791, on the device). For the listed groups (width >= 2):
+ *   etm_prefix_counts  out_counts int64 [n_work] = rows holding the group's prefix
+ *                      (popcount of the AND of its width-1 prefix columns);
+ *   etm_prefix_rows    out_rows int32 = those rows, ascending, group wi at
+ *                      [row_off[wi], row_off[wi+1]) (row_off: exclusive prefix of
+ *                      the counts);
+ *   etm_project        member i of group wi -> cbuf[cbase[wi] + i*cld[wi] ...]:
+ *                      its column's bits at the prefix rows, 64 per word, zero
+ *                      padded to cld[wi] words (cld % 32 == 0, cbase even);
+ *                      mem_off int64 [n_work+1] = exclusive prefix of group sizes.
+ *   etm_count_tiles_proj  etm_count_tiles over the projected words
+ *                      (cwords[wi] words per member; no prefix AND).
+ */
+int etm_prefix_counts(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                      const int64_t* grp_first, const int64_t* work_groups, int64_t n_work, int64_t* out_counts,
+                      void* stream);
+int etm_prefix_rows(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                    const int64_t* grp_first, const int64_t* work_groups, int64_t n_work, const int64_t* row_off,
+                    int32_t* out_rows, void* stream);
+int etm_project(const uint64_t* fbv, int64_t ld, const int32_t* rows, int32_t width, const int64_t* grp_first,
+                const int64_t* work_groups, const int64_t* mem_off, int64_t n_work, const int64_t* row_off,
+                const int32_t* row_idx, const int64_t* cbase, const int64_t* cld, uint64_t* cbuf, void* stream);
+int etm_count_tiles_proj(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
+                         const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
+                         const int64_t* work_off, int64_t n_work, int64_t chunk_base, const uint8_t* cls,
+                         int32_t method, int32_t* out_counts, void* stream);
+
+/*
  * Survivors of a counted chunk (groups [g0, g1)), in candidate order, decoded
  * into rows of width+1 columns. Replaces threshold_filter
  * (gpu/kernels/filter.py:85-120), decode_k2_pairs_flat / decode_k3plus_flat

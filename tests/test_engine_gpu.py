@@ -29,6 +29,8 @@ def engines(pkg):
         "batched": eng.Engine(form="batched"),
         "plain": eng.Engine(form="plain"),
         "tiny": eng.Engine(form="batched", chunk_cands=97, small_group=3),
+        "proj": eng.Engine(form="batched", small_group=2, proj_density=1.01, proj_bytes=1 << 14),
+        "noproj": eng.Engine(form="batched", project=False),
     }
 
 
@@ -47,7 +49,7 @@ def test_transactions_match_golden(pkg, golden_cases, engines, name):
         assert pairs == want
 
 
-@pytest.mark.parametrize("form", ["plain", "tiny"])
+@pytest.mark.parametrize("form", ["plain", "tiny", "proj", "noproj"])
 @pytest.mark.parametrize("name", ["implication_plain", "implication_prune", "implication_infer", "plain_small_plain",
                                   "deep_sparse_small", "dense_k2_small", "word_tail_65"])
 def test_forms_match_golden(pkg, golden_cases, engines, name, form):

@@ -233,5 +233,10 @@ def test_compaction_overflow_regrows(pkg):
     fbv, ldp = eng.gather(dev.data_ptr(), n_words, np.arange(n_f), n_words)
     gen = engm.Level(torch.arange(n_f, dtype=torch.int32, device="cuda")[:, None].contiguous(),
                      torch.ones(n_f, dtype=torch.int32, device="cuda"))
+    # Every pair survives at min_count 1 (random 256-bit columns always share a bit), far past the
+    # first output capacity (65,536 rows), so the compaction regrows its output and repeats.
     new, stats = eng.count_level(gen, fbv, ldp, n_words, 1, False, False)
-    assert new.n == n_f * (n_f - 1) // 2 and stats.n_chunks > 100
+    ii, jj = np.triu_indices(n_f, 1)
+    want = np.bitwise_count(bv.view(np.uint64)[ii] & bv.view(np.uint64)[jj]).sum(axis=1)
+    assert new.n == len(ii) and stats.n_frequent == len(ii)
+    assert np.array_equal(new.counts.cpu().numpy(), want)
