@@ -116,36 +116,68 @@ def dense_k2_device(pkg, lib, spec):
     return bv.view(torch.uint64)
 
 
-def cpu_sample(pkg, spec, budget_s: float = 20.0) -> dict:
-    """The CPU oracle on a bounded slice of the workload (same items and thresholds, fewer rows),
-    extrapolated linearly in rows to the full workload."""
+#: Candidates per level of each workload (K=1 columns, K=2 pairs, K=3 prefix-group pairs), as the engine
+#: enumerates them; the engine arm asserts its own counts against these on every run.
+LEVEL_CANDIDATES = {
+    "dense_k2": [4096, 8_345_655, 5_155_139_504],
+    "dense_k2_mid": None,
+    "dense_k2_small": [1024, 522_753, 73_706_695],
+}
+
+
+def cpu_estimate(spec, level_cands, budget_s: float = 12.0, bv_host=None) -> dict:
+    """Seconds the CPU oracle's counting would take on the whole workload, from a timed sample.
+
+    The oracle counts a candidate by ANDing its k column bitvectors and
+    popcounting (count_per_candidate, core/cpu_miner.py:794-809), a cost
+    that depends on k and the words per column, not on the bits. Per level
+    a sample of candidates over full-length columns (the workload's own when
+    ``bv_host`` is given, else random words of the same length) is timed and
+    scaled by the level's candidate count; K=1 is one popcount per column.
+    """
     from oracle import miner
 
-    syn = pkg.synthetic
-    p = syn.dense_k2_probs(spec["n_items"], seed=spec["seed"])
-    thr = syn.bernoulli_thresholds(p)
-    rows = 2048
-    best = None
-    while True:
-        bv = syn.bernoulli_bitvecs(thr, rows, spec["hash_seed"])
-        t0 = time.perf_counter()
-        miner.mine_bitvecs(bv, rows, spec["min_support"], spec["max_length"])
-        dt = time.perf_counter() - t0
-        best = (rows, dt)
-        if dt > budget_s / 4 or rows >= spec["n_rows"]:
-            break
-        rows = min(spec["n_rows"], rows * 4)
-    rows, dt = best
-    scale = spec["n_rows"] / rows
-    return {"value": dt * scale, "unit": "s", "cores": 1, "kind": "port",
-            "sample": f"oracle/miner.py mine_bitvecs on the first {rows:,} of {spec['n_rows']:,} rows "
-                      f"(same items and thresholds, min_support {spec['min_support']}), {dt:.2f} s, "
-                      f"extrapolated x{scale:.0f} in rows"}
+    n_words = (spec["n_rows"] + 63) // 64
+    rng = np.random.default_rng(1)
+    if bv_host is None:
+        n_s = 128
+        bv = rng.integers(0, 2**63, size=(n_s, n_words), dtype=np.int64).view(np.uint64)
+    else:
+        n_s = min(128, bv_host.shape[0])
+        bv = np.ascontiguousarray(bv_host[:n_s])
+    per_level = []
+    total = 0.0
+    t_k1 = time.perf_counter()
+    miner.popcount_rows(bv)
+    t_k1 = (time.perf_counter() - t_k1) / n_s
+    total += t_k1 * level_cands[0]
+    per_level.append({"k": 1, "candidates": level_cands[0], "s_per_candidate": t_k1})
+    for k, n_c in enumerate(level_cands[1:], start=2):
+        sample = 256
+        while True:
+            sets = np.sort(np.stack([rng.choice(n_s, size=k, replace=False) for _ in range(sample)]), axis=1)
+            t0 = time.perf_counter()
+            miner.count_itemsets(sets.astype(np.int32), bv)
+            dt = time.perf_counter() - t0
+            if dt > budget_s / (2 * len(level_cands)) or sample >= 65536:
+                break
+            sample *= 4
+        per = dt / sample
+        total += per * n_c
+        per_level.append({"k": k, "candidates": n_c, "s_per_candidate": per, "sampled": sample})
+    return {"value": total, "unit": "s", "cores": 1, "kind": "port",
+            "sample": "oracle/miner.py count_itemsets (AND + popcount per candidate, core/cpu_miner.py:794-809) "
+                      f"timed on sampled candidates over {n_words:,}-word columns, scaled by each level's "
+                      "candidate count",
+            "levels": per_level}
 
 
 def run_reference(args, spec) -> None:
-    pkg = _pkg()
-    base = cpu_sample(pkg, spec, budget_s=max(5.0, 20.0 / max(1, args.steps)))
+    cands = LEVEL_CANDIDATES.get(args.workload)
+    if cands is None:
+        print(json.dumps({"impl": "reference", "unavailable": f"no recorded candidate counts for {args.workload}"}))
+        return
+    base = cpu_estimate(spec, cands, budget_s=max(6.0, 30.0 / max(1, args.steps + args.warmup)))
     line = {
         "impl": "reference", "metric": METRIC, "value": base["value"], "unit": "s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["value"] * 1e3, "higher_is_better": False,
@@ -286,8 +318,12 @@ def main() -> None:
                 "ms_per_step": top["ms"] / args.steps, "share_of_step": (top["ms"] / args.steps) / ms}
 
     cpu = None
+    level_cands = [s.n_candidates for s in out.stats]
+    recorded = LEVEL_CANDIDATES.get(args.workload)
+    if recorded is not None:
+        assert level_cands == recorded, (level_cands, recorded)
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_sample(pkg, spec)
+        cpu = cpu_estimate(spec, level_cands, bv_host=bv[:128].view(torch.int64).cpu().numpy().view(np.uint64))
 
     if rank == 0:
         line = {
