@@ -1,13 +1,404 @@
 // Exact 0/1 Gram of prefix-group suffixes on the tcgen05 tensor cores.
+//
+// For a group whose members are bit rows x_0..x_{m-1} (projected suffix
+// words, or for K=2 the frequent columns themselves), the pair counts are
+// C[i][j] = popcount(x_i & x_j) = sum_r x_i[r] * x_j[r]: the Gram matrix X X^T
+// of a 0/1 matrix. One CTA per SM walks tile-pairs (ti <= tj) of 128 x 128
+// members:
+//
+//   warps 0-3  producers: per stage (K = 64 transactions for f16, 128 for
+//              e4m3) each thread loads its A row's and B row's words and
+//              expands every bit into a 0.0/1.0 element, writing the 128-byte
+//              swizzled K-major operand layout the MMA reads (SWIZZLE_128B);
+//              then fence.proxy.async and an mbarrier arrive.
+//   warp 4     one thread issues tcgen05.mma (M=128, N=128) per 16/32-element
+//              K step into a TMEM f32 accumulator, and tcgen05.commit frees
+//              each stage and finally signals the epilogue.
+//   warps 0-3  epilogue: tcgen05.ld of their 32 TMEM lanes, f32 -> int32,
+//              the i < j pair counts written at their lexicographic slots.
+//
+// Exactness: every product is 0 or 1 and every partial sum is an integer
+// below 2^24 (the caller sends only groups of at most 2^24 rows here), so the
+// f32 accumulation is exact. Diagonal tile-pairs load one operand and use it
+// for both A and B.
+//
+// Every mbarrier wait is bounded: after WAIT_LIMIT polls the block raises an
+// abort flag, every thread leaves its loop, the MMA thread waits (bounded) for
+// its issued MMAs, TMEM is freed, and the kernel records ETM_ETIMEOUT in its
+// status word instead of hanging.
 #include "etm_count.cuh"
 
+namespace {
+
+using namespace etm;
+
+constexpr int TC_M = 128;
+constexpr int TC_N = 128;
+constexpr int TC_STAGES = 4;
+constexpr int TC_PRODUCERS = 128;
+constexpr int TC_THREADS = TC_PRODUCERS + 32;
+constexpr uint32_t TC_TMEM_COLS = 128;
+constexpr int ATOM_BYTES = 128 * 128;  // 128 rows x 128 bytes, one SWIZZLE_128B K block
+constexpr int SLOT_BYTES = 2 * ATOM_BYTES;
+constexpr int TC_SMEM_BYTES = TC_STAGES * SLOT_BYTES + 1024;
+constexpr long long WAIT_LIMIT = 1LL << 25;
+
+__device__ int g_tc_status;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase of `parity` to complete; false if the block aborts or the wait runs out.
+__device__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+    long long n = 0;
+    while (!mbar_test(bar, parity)) {
+        if (*abort_flag) return false;
+        if (++n > WAIT_LIMIT) {
+            *abort_flag = 1;
+            return false;
+        }
+        if (n > 32) __nanosleep(64);
+    }
+    return true;
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major, SWIZZLE_128B, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;                  // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;        // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                  // descriptor version for tcgen05
+    d |= (uint64_t)2 << 61;                  // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor: D f32, A/B format code 0 (f16 for kind::f16, e4m3 for kind::f8f6f4),
+// both K-major, N = 128, M = 128.
+__host__ __device__ constexpr uint32_t instr_desc() {
+    return (1u << 4) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+}
+
+template <int ELEM>
+__device__ __forceinline__ void mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc) {
+    if constexpr (ELEM == 2) {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(a), "l"(b), "r"(instr_desc()), "r"(acc));
+    } else {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(a), "l"(b), "r"(instr_desc()), "r"(acc));
+    }
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// 16 bytes of operand elements from bits [0, 16/ELEM) of v: 1.0 (f16 0x3C00 / e4m3 0x38) or 0.
+template <int ELEM>
+__device__ __forceinline__ uint4 expand_chunk(uint32_t v) {
+    uint4 o;
+    if constexpr (ELEM == 2) {
+        // 8 bits -> 8 halves: two bits per 32-bit word.
+        uint32_t w[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t t = (v >> (2 * q)) & 3u;
+            w[q] = ((t & 1u) * 0x3C00u) | ((t >> 1) * 0x3C000000u);
+        }
+        o = make_uint4(w[0], w[1], w[2], w[3]);
+    } else {
+        // 16 bits -> 16 bytes: four bits per 32-bit word, spread to one bit per byte, times 0x38.
+        uint32_t w[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t nib = (v >> (4 * q)) & 0xFu;
+            w[q] = ((nib * 0x00204081u) & 0x01010101u) * 0x38u;
+        }
+        o = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    return o;
+}
+
+// Row r of a 128 x 128-byte SWIZZLE_128B atom: logical 16-byte chunk c lives at chunk c ^ (r % 8).
+template <int ELEM>
+__device__ __forceinline__ void store_row(uint8_t* atom, int r, uint64_t x0, uint64_t x1) {
+    uint8_t* row = atom + (r >> 3) * 1024 + (r & 7) * 128;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        uint32_t bits;
+        if constexpr (ELEM == 2) bits = (uint32_t)(x0 >> (8 * c)) & 0xFFu;
+        else bits = (uint32_t)((c < 4 ? x0 : x1) >> (16 * (c & 3))) & 0xFFFFu;
+        *reinterpret_cast<uint4*>(row + ((c ^ (r & 7)) << 4)) = expand_chunk<ELEM>(bits);
+    }
+}
+
+template <int ELEM>
+__global__ void __launch_bounds__(TC_THREADS, 1) gram_tc_kernel(
+    const uint64_t* __restrict__ src, const int64_t* __restrict__ cbase, const int64_t* __restrict__ cwords,
+    const int64_t* __restrict__ cld, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
+    const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
+    const uint8_t* __restrict__ cls, int32_t* __restrict__ out) {
+    constexpr int WORDS_PER_STAGE = ELEM == 2 ? 1 : 2;  // a 128-byte row holds 64 halves or 128 bytes
+    extern __shared__ uint8_t dsmem[];
+    __shared__ __align__(8) uint64_t full_bar[TC_STAGES];
+    __shared__ __align__(8) uint64_t empty_bar[TC_STAGES];
+    __shared__ __align__(8) uint64_t acc_bar;
+    __shared__ __align__(8) uint64_t drain_bar;
+    __shared__ uint32_t tmem_sh;
+    __shared__ int abort_sh;
+    __shared__ int64_t off_a[TC_M];
+    __shared__ int64_t off_b[TC_N];
+
+    uint8_t* slots = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) {
+        for (int s = 0; s < TC_STAGES; s++) {
+            mbar_init(&full_bar[s], TC_PRODUCERS);
+            mbar_init(&empty_bar[s], 1);
+        }
+        mbar_init(&acc_bar, 1);
+        mbar_init(&drain_bar, 1);
+        abort_sh = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 4) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_sh)),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        tc_fence_before();
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_sh;
+    volatile int* abort_flag = &abort_sh;
+
+    const int64_t total = work_off[n_work];
+    int64_t gstage = 0;      // stages issued so far (barrier phases)
+    uint32_t tile_iter = 0;  // tiles whose accumulator was committed
+
+    for (int64_t tp = blockIdx.x; tp < total; tp += gridDim.x) {
+        const int64_t wi = upper_find(work_off, n_work, tp);
+        const int64_t g = work_groups[wi];
+        const int64_t m = grp_size[g];
+        const int64_t nt = ceil_div<int64_t>(m, TC_M);
+        int64_t ti, tj1;
+        tri_decode(tp - work_off[wi], nt + 1, &ti, &tj1);
+        const int64_t tj = tj1 - 1;
+        const bool diag = ti == tj;
+        const int64_t cb = cand_off[g] - chunk_base;
+        const int64_t words = cwords[wi];
+        const int64_t n_stages = ceil_div<int64_t>(words, WORDS_PER_STAGE);
+        if (tid < TC_M) {
+            const int64_t ia = ti * TC_M + tid, ib = tj * TC_N + tid;
+            off_a[tid] = ia < m ? cbase[wi] + ia * cld[wi] : -1;
+            off_b[tid] = ib < m ? cbase[wi] + ib * cld[wi] : -1;
+        }
+        int any = cls == nullptr;
+        if (!any && tid < TC_M) {
+            const int64_t i = ti * TC_M + tid;
+            for (int c = 0; c < TC_N && !any; c++) {
+                const int64_t j = tj * TC_N + c;
+                any = i < j && j < m && cls[cb + tri_index(i, j, m)] == ETM_CAND_COUNT;
+            }
+        }
+        if (!__syncthreads_or(any)) continue;
+
+        if (warp < 4) {
+            // ---- producers ----
+            const int64_t oa = off_a[tid], ob = off_b[tid];
+            for (int64_t s = 0; s < n_stages && !*abort_flag; s++) {
+                const int64_t G = gstage + s;
+                const int slot = (int)(G % TC_STAGES);
+                const uint32_t use = (uint32_t)(G / TC_STAGES);
+                if (!mbar_wait(&empty_bar[slot], (use & 1u) ^ 1u, abort_flag)) break;
+                const int64_t w0 = s * WORDS_PER_STAGE;
+                uint64_t a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+                if (oa >= 0) {
+                    a0 = __ldg(src + oa + w0);
+                    if (WORDS_PER_STAGE == 2) a1 = __ldg(src + oa + w0 + 1);
+                }
+                uint8_t* slot_base = slots + slot * SLOT_BYTES;
+                store_row<ELEM>(slot_base, tid, a0, a1);
+                if (!diag) {
+                    if (ob >= 0) {
+                        b0 = __ldg(src + ob + w0);
+                        if (WORDS_PER_STAGE == 2) b1 = __ldg(src + ob + w0 + 1);
+                    }
+                    store_row<ELEM>(slot_base + ATOM_BYTES, tid, b0, b1);
+                }
+                fence_proxy_async();
+                mbar_arrive(&full_bar[slot]);
+            }
+            // ---- epilogue ----
+            const bool ok = n_stages == 0 || mbar_wait(&acc_bar, tile_iter & 1u, abort_flag);
+            if (ok) {
+                tc_fence_after();
+                const int64_t i = ti * TC_M + warp * 32 + lane;
+                for (int q = 0; q < TC_N / 32; q++) {
+                    uint32_t v[32];
+                    if (n_stages > 0) {
+                        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(q * 32);
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+                            "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                              "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+                              "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+                              "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                            : "r"(taddr));
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < 32; c++) v[c] = 0u;
+                    }
+                    if (i < m) {
+#pragma unroll
+                        for (int c = 0; c < 32; c++) {
+                            const int64_t j = tj * TC_N + q * 32 + c;
+                            if (i < j && j < m) {
+                                const int64_t t = cb + tri_index(i, j, m);
+                                if (cls == nullptr || cls[t] == ETM_CAND_COUNT)
+                                    out[t] = n_stages > 0 ? __float2int_rn(__uint_as_float(v[c])) : 0;
+                            }
+                        }
+                    }
+                }
+            }
+            tc_fence_before();
+        } else if (lane == 0) {
+            // ---- MMA issuer ----
+            tc_fence_after();
+            for (int64_t s = 0; s < n_stages; s++) {
+                const int64_t G = gstage + s;
+                const int slot = (int)(G % TC_STAGES);
+                const uint32_t use = (uint32_t)(G / TC_STAGES);
+                if (!mbar_wait(&full_bar[slot], use & 1u, abort_flag)) break;
+                tc_fence_after();
+                const uint32_t a_addr = smem_u32(slots + slot * SLOT_BYTES);
+                const uint32_t b_addr = diag ? a_addr : a_addr + ATOM_BYTES;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {  // 4 x 32 bytes of K per 128-byte row
+                    mma<ELEM>(tmem, smem_desc(a_addr + 32 * k), smem_desc(b_addr + 32 * k), (s > 0 || k > 0) ? 1u : 0u);
+                }
+                mma_commit(&empty_bar[slot]);
+            }
+            mma_commit(&acc_bar);
+        }
+        gstage += n_stages;
+        tile_iter += 1;
+        __syncthreads();
+        if (*abort_flag) break;
+    }
+
+    // Teardown: make sure no MMA is still writing TMEM, then free it.
+    if (warp == 4) {
+        if (lane == 0 && *abort_flag) {
+            mma_commit(&drain_bar);
+            long long n = 0;
+            while (!mbar_test(&drain_bar, 0) && ++n < WAIT_LIMIT) __nanosleep(64);
+        }
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+    }
+    if (tid == 0 && *abort_flag) atomicExch(&g_tc_status, ETM_ETIMEOUT);
+}
+
+template <int ELEM>
+int launch_gram(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
+                const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
+                int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t* out,
+                cudaStream_t s) {
+    static bool configured = false;
+    if (!configured) {
+        ETM_CUDA(cudaFuncSetAttribute(gram_tc_kernel<ELEM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      TC_SMEM_BYTES));
+        configured = true;
+    }
+    const int64_t sms = max(1, sm_count());
+    const int grid = (int)max64(1, min64(sms, n_tiles > 0 ? n_tiles : sms));
+    gram_tc_kernel<ELEM><<<grid, TC_THREADS, TC_SMEM_BYTES, s>>>(cbuf, cbase, cwords, cld, grp_size, cand_off,
+                                                                 work_groups, work_off, n_work, chunk_base, cls, out);
+    ETM_LAUNCHED("gram_tc");
+    return ETM_OK;
+}
+
+}  // namespace
+
 namespace etm {
+
+int gram_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
+            const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
+            int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t elem, int32_t* out,
+            cudaStream_t s) {
+    if (elem == 2)
+        return launch_gram<2>(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, n_tiles,
+                              chunk_base, cls, out, s);
+    ETM_REQUIRE(elem == 1, ETM_EINVAL, "gram_tc: element size %d (1 = e4m3, 2 = f16)", elem);
+    return launch_gram<1>(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, n_tiles,
+                          chunk_base, cls, out, s);
+}
 
 int count_tiles_tensor(const uint64_t*, int64_t, int64_t, const int32_t*, int32_t, const int64_t*, const int32_t*,
                        const int64_t*, const int64_t*, const int64_t*, int64_t, int64_t, const uint8_t*, int32_t*,
                        cudaStream_t) {
-    set_error("etm_count_tiles: the tensor-core method is not built in this library");
+    set_error("etm_count_tiles: the tensor method counts projected groups; use etm_count_tiles_tc");
     return ETM_EINVAL;
 }
 
 }  // namespace etm
+
+extern "C" int etm_count_tiles_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords,
+                                  const int64_t* cld, const int32_t* grp_size, const int64_t* cand_off,
+                                  const int64_t* work_groups, const int64_t* work_off, int64_t n_work,
+                                  int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t elem,
+                                  int32_t* out_counts, void* stream) {
+    ETM_REQUIRE((reinterpret_cast<uintptr_t>(cbuf) & 15) == 0, ETM_EINVAL, "etm_count_tiles_tc: cbuf must be 16-byte aligned");
+    if (n_work <= 0) return ETM_OK;
+    return etm::gram_tc(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, n_tiles,
+                        chunk_base, cls, elem, out_counts, as_stream(stream));
+}
+
+extern "C" int etm_device_status(void* stream) {
+    int v = 0;
+    ETM_CUDA(cudaMemcpyFromSymbolAsync(&v, g_tc_status, sizeof(int), 0, cudaMemcpyDeviceToHost, as_stream(stream)));
+    ETM_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    if (v != 0) {
+        const int zero = 0;
+        ETM_CUDA(cudaMemcpyToSymbolAsync(g_tc_status, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, as_stream(stream)));
+        ETM_CUDA(cudaStreamSynchronize(as_stream(stream)));
+        etm::set_error("a tensor-core counting kernel gave up a bounded wait (status %d)", v);
+    }
+    return v;
+}

@@ -47,6 +47,10 @@ CHUNK_CANDS = 1 << 27
 PROJ_DENSITY = 0.5
 #: Device bytes of projected suffix words (and row lists) per chunk.
 PROJ_BYTES = 4 << 30
+#: Members per tile side of the tensor-core Gram kernel.
+TC_TILE = 128
+#: Largest group (rows) the tensor-core Gram counts exactly: f32 holds every integer up to 2^24.
+TC_MAX_ROWS = 1 << 24
 #: Counting method for tile-pairs: "popcount" or "tensor".
 DEFAULT_METHOD = "popcount"
 
@@ -185,7 +189,8 @@ class Engine:
 
     def __init__(self, device: torch.device | int | None = None, *, method: str = DEFAULT_METHOD,
                  form: str = "batched", chunk_cands: int = CHUNK_CANDS, small_group: int = SMALL_GROUP,
-                 project: bool = True, proj_density: float = PROJ_DENSITY, proj_bytes: int = PROJ_BYTES):
+                 project: bool = True, proj_density: float = PROJ_DENSITY, proj_bytes: int = PROJ_BYTES,
+                 tc_elem: int = 2):
         if not torch.cuda.is_available():
             raise RuntimeError("the GB300 engine needs a CUDA device; there is no CPU fallback")
         self.lib = load_library()
@@ -202,14 +207,17 @@ class Engine:
         self.project = bool(project)
         self.proj_density = float(proj_density)
         self.proj_bytes = int(proj_bytes)
+        #: Tensor-core operand element: 2 = f16 (kind::f16), 1 = e4m3 (kind::f8f6f4).
+        self.tc_elem = int(tc_elem)
         self.scratch = _Scratch(self.device)
         self.launches = 0
         #: When set, every counting / compaction launch is bracketed by CUDA events on its stream.
         self.profile_kernels = False
-        self._events: list[tuple[str, object, object, int]] = []
+        self._events: list[tuple] = []
+        self.used_tensor = False
 
     # -- kernel timing ----------------------------------------------------------
-    def _launch(self, name: str, nbytes: int, fn):
+    def _launch(self, name: str, nbytes: int, fn, flops: float = 0.0):
         """Run ``fn`` (one library call), timing it with CUDA events when profiling."""
         if not self.profile_kernels:
             return fn()
@@ -218,7 +226,7 @@ class Engine:
         e0.record()
         st = fn()
         e1.record()
-        self._events.append((name, e0, e1, int(nbytes)))
+        self._events.append((name, e0, e1, int(nbytes), float(flops)))
         return st
 
     def reset_kernel_times(self) -> None:
@@ -228,13 +236,15 @@ class Engine:
         """Per kernel: launches, total ms (CUDA events on the launching stream), algorithmic bytes."""
         torch.cuda.synchronize()
         out: dict[str, dict] = {}
-        for name, e0, e1, nbytes in self._events:
-            r = out.setdefault(name, {"name": name, "launches": 0, "ms": 0.0, "bytes": 0})
+        for name, e0, e1, nbytes, flops in self._events:
+            r = out.setdefault(name, {"name": name, "launches": 0, "ms": 0.0, "bytes": 0, "flops": 0.0})
             r["launches"] += 1
             r["ms"] += e0.elapsed_time(e1)
             r["bytes"] += nbytes
+            r["flops"] += flops
         for r in out.values():
             r["gbs"] = r["bytes"] / (r["ms"] / 1e3) / 1e9 if r["ms"] > 0 else 0.0
+            r["tflops"] = r["flops"] / (r["ms"] / 1e3) / 1e12 if r["ms"] > 0 else 0.0
         return out
 
     # -- K = 1 -----------------------------------------------------------------
@@ -297,7 +307,8 @@ class Engine:
         np.cumsum(m, out=mem_off[1:])
         cb = np.zeros(len(gids) + 1, np.int64)
         np.cumsum(m * cl, out=cb[1:])
-        nt = (m + TILE - 1) // TILE
+        tile = TC_TILE if method == 1 else TILE
+        nt = (m + tile - 1) // tile
         toff = np.zeros(len(gids) + 1, np.int64)
         np.cumsum(nt * (nt + 1) // 2, out=toff[1:])
         n = len(gids)
@@ -317,12 +328,25 @@ class Engine:
                                                        _p(mo), n, _p(ro), _p(rowidx), _p(cbase), _p(cld), _p(cbuf),
                                                        _stream()))
         check(st, "etm_project")
-        st = self._launch("count_tiles_proj", int((m * cw).sum() * 8),
-                          lambda: self.lib.etm_count_tiles_proj(_p(cbuf), _p(cbase), _p(cwords), _p(cld),
-                                                                _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, base,
-                                                                _p(cls), method, _p(counts), _stream()))
-        check(st, "etm_count_tiles_proj")
-        self.launches += 3
+        self._count_words(cbuf, cbase, cwords, cld, grp_size, cand_off, wg, wo, n, int(toff[-1]), base, cls, counts,
+                          method, int((m * cw).sum() * 8), float(((m.astype(np.float64) ** 2) * cw * 64).sum()))
+        self.launches += 2
+
+    def _count_words(self, cbuf, cbase, cwords, cld, grp_size, cand_off, wg, wo, n, n_tiles, base, cls, counts,
+                     method, nbytes, macs):
+        """Tile-pair counts over member words laid out as cbuf[cbase[wi] + i * cld[wi]]: tensor or popcount."""
+        if method == 1:
+            st = self._launch("gram_tc", nbytes, lambda: self.lib.etm_count_tiles_tc(
+                _p(cbuf), _p(cbase), _p(cwords), _p(cld), _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, n_tiles,
+                base, _p(cls), self.tc_elem, _p(counts), _stream()), flops=2 * macs)
+            check(st, "etm_count_tiles_tc")
+            self.used_tensor = True
+        else:
+            st = self._launch("count_tiles_proj", nbytes, lambda: self.lib.etm_count_tiles_proj(
+                _p(cbuf), _p(cbase), _p(cwords), _p(cld), _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, base,
+                _p(cls), 0, _p(counts), _stream()))
+            check(st, "etm_count_tiles_proj")
+        self.launches += 1
 
     def count_level(self, gen: Level, fbv: torch.Tensor, ldp: int, n_words: int, mc: int,
                     infer: bool, prune: bool, n_rows: int | None = None) -> tuple[Level, LevelStats]:
@@ -351,12 +375,17 @@ class Engine:
         classify = (infer or prune) and width >= 2
         mode = (1 if prune or infer else 0) | (2 if infer else 0)
         big = sizes > self.small_group
+        tensor = self.method == "tensor"
         pcnt = np.zeros(G, np.int64)
         proj = np.zeros(G, bool)
-        if self.project and width >= 2 and big.any():
+        if (self.project or tensor) and width >= 2 and big.any():
             ids_big = np.flatnonzero(big)
             pcnt[ids_big] = self.prefix_counts(fbv, ldp, n_words, gen, grp_first, ids_big)
-            proj = big & (pcnt < self.proj_density * n_rows)
+            if tensor:
+                # The tensor cores count projected words; a prefix past 2^24 rows stays on popcount.
+                proj = big & (pcnt <= TC_MAX_ROWS)
+            else:
+                proj = big & (pcnt < self.proj_density * n_rows)
         pwords = np.maximum(32, ((pcnt + 63) // 64 + 31) // 32 * 32)
         pbytes = np.where(proj, sizes * pwords * 8 + pcnt * 4, 0)
         pcum = np.zeros(G + 1, np.int64)
@@ -367,7 +396,9 @@ class Engine:
         acc = self.scratch.get("acc", 1, torch.int64)
         acc.zero_()
         n_out = 0
-        method = 1 if self.method == "tensor" else 0
+        method = 1 if tensor else 0
+        # K=2 on the tensor cores: the one group of every generator, its members the padded columns.
+        whole_tc = tensor and width == 1 and n_rows <= TC_MAX_ROWS
         g0 = 0
         while g0 < G:
             # Chunk: whole groups within both budgets (at least one group).
@@ -390,6 +421,20 @@ class Engine:
             for kind, sel in (("cands", small), ("tiles", ~small & ~pr), ("proj", pr)):
                 gids = ids[sel]
                 if len(gids) == 0:
+                    continue
+                if kind == "tiles" and whole_tc:
+                    mg = sizes[gids]
+                    nt = (mg + TC_TILE - 1) // TC_TILE
+                    toff = np.zeros(len(gids) + 1, np.int64)
+                    np.cumsum(nt * (nt + 1) // 2, out=toff[1:])
+                    n = len(gids)
+                    host = np.concatenate([gids, toff, np.zeros(n, np.int64), np.full(n, n_words, np.int64),
+                                           np.full(n, ldp, np.int64)])
+                    d = torch.from_numpy(host).to(self.device)
+                    self._count_words(fbv, d[2 * n + 1:3 * n + 1], d[3 * n + 1:4 * n + 1], d[4 * n + 1:5 * n + 1],
+                                      grp_size, cand_off, d[:n], d[n:2 * n + 1], n, int(toff[-1]), base, cls, counts,
+                                      1, int(mg.sum()) * n_words * 8,
+                                      float((mg.astype(np.float64) ** 2).sum() * n_words * 64))
                     continue
                 if kind == "proj":
                     groups = [gids] if self.form == "batched" else [gids[q:q + 1] for q in range(len(gids))]
@@ -440,6 +485,10 @@ class Engine:
             n_out = new_total
             stats.n_chunks += 1
             g0 = g1
+        if self.used_tensor:
+            st = self.lib.etm_device_status(_stream())
+            if st != 0:
+                raise RuntimeError(f"tensor-core counting failed: {self.lib.etm_last_error().decode()}")
         level = Level(out_rows[:n_out], out_counts[:n_out])
         stats.n_frequent = n_out
         stats.ms = (time.perf_counter() - t0) * 1e3
@@ -526,5 +575,5 @@ class Engine:
 def mine(bitvecs, n_rows: int, min_support: float, max_length: int | None = None, **kw) -> MineOutput:
     """Mine device bitvectors [n_cols, ceil(N/64)] with a fresh ``Engine`` (see ``Engine.mine``)."""
     engine_kw = {k: kw.pop(k) for k in ("method", "form", "chunk_cands", "small_group", "device", "project",
-                                        "proj_density", "proj_bytes") if k in kw}
+                                        "proj_density", "proj_bytes", "tc_elem") if k in kw}
     return Engine(**engine_kw).mine(bitvecs, n_rows, min_support, max_length, **kw)

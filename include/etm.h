@@ -179,6 +179,27 @@ int etm_count_tiles_proj(const uint64_t* cbuf, const int64_t* cbase, const int64
                          int32_t method, int32_t* out_counts, void* stream);
 
 /*
+ * etm_count_tiles_proj on the tcgen05 tensor cores: the pair counts of each
+ * listed group are the Gram matrix of its 0/1 member words, computed by
+ * 128 x 128 tile-pairs with bits expanded in shared memory to f16 (elem 2,
+ * kind::f16) or e4m3 (elem 1, kind::f8f6f4) and f32 accumulation in TMEM.
+ * Exact while every group has at most 2^24 rows (cwords <= 262144): the caller
+ * sends larger groups to the popcount kernels. work_off counts tile-pairs of
+ * 128 members: T(T+1)/2, T = ceil(m/128); n_tiles = work_off[n_work] (sizes
+ * the grid). New in this engine (the reference counts on CUDA cores only).
+ */
+int etm_count_tiles_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
+                       const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
+                       const int64_t* work_off, int64_t n_work, int64_t n_tiles, int64_t chunk_base,
+                       const uint8_t* cls, int32_t elem, int32_t* out_counts, void* stream);
+
+/*
+ * Reads and clears the device status word the tensor-core kernels raise when a
+ * bounded wait gives up (synchronizes `stream`). Returns 0, or ETM_ETIMEOUT.
+ */
+int etm_device_status(void* stream);
+
+/*
  * Survivors of a counted chunk (groups [g0, g1)), in candidate order, decoded
  * into rows of width+1 columns. Replaces threshold_filter
  * (gpu/kernels/filter.py:85-120), decode_k2_pairs_flat / decode_k3plus_flat
