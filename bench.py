@@ -206,6 +206,7 @@ def main() -> None:
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="dense_k2", choices=sorted(WORKLOADS))
     ap.add_argument("--method", default=None, choices=["popcount", "tensor"])
+    ap.add_argument("--tc-elem", type=int, default=1, choices=[1, 2], help="tensor operands: 1 = e4m3, 2 = f16")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparator")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     args = ap.parse_args()
@@ -236,7 +237,7 @@ def main() -> None:
     method = args.method or engm.DEFAULT_METHOD
     bv = dense_k2_device(pkg, lib, spec)
     n_rows = spec["n_rows"]
-    eng = engm.Engine(form="batched", method=method)
+    eng = engm.Engine(form="batched", method=method, tc_elem=args.tc_elem)
     eng.profile_kernels = True
 
     def one(e):
@@ -276,7 +277,7 @@ def main() -> None:
     # Plain form (one counting launch per prefix group): the comparator.
     plain = None
     if not args.no_plain:
-        pe = engm.Engine(form="plain", method=method)
+        pe = engm.Engine(form="plain", method=method, tc_elem=args.tc_elem)
         one(pe)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -311,11 +312,22 @@ def main() -> None:
     roof = None
     if kern:
         top = max(kern.values(), key=lambda r: r["ms"])
-        achieved = top["bytes"] / (top["ms"] / top["launches"] / 1e3) / top["launches"] / 1e9 if top["ms"] > 0 else 0.0
-        roof = {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": peaks["hbm_gbs"],
-                "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                "traffic": None, "launches_per_step": top["launches"] / args.steps,
-                "ms_per_step": top["ms"] / args.steps, "share_of_step": (top["ms"] / args.steps) / ms}
+        per_launch_s = top["ms"] / top["launches"] / 1e3
+        if top["name"] == "gram_tc":
+            # Useful work: 2 x C(m,2) x rows per group; the e4m3 MMAs run at twice the dense bf16 rate.
+            fp8 = method == "tensor" and eng.tc_elem == 1
+            peak = peaks["bf16_tflops"] * (2.0 if fp8 else 1.0)
+            achieved = top["flops"] / top["launches"] / per_launch_s / 1e12
+            roof = {"bound": "tensor", "kernel": top["name"], "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak,
+                    "peak_source": f"{peaks['source']} bf16 dense" + (" x 2 (e4m3 operands)" if fp8 else ""),
+                    "work": "2 * C(m,2) * rows per prefix group (upper-triangle pair counts)"}
+        else:
+            achieved = top["bytes"] / top["launches"] / per_launch_s / 1e9
+            roof = {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": peaks["hbm_gbs"],
+                    "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"]}
+        roof.update({"traffic": None, "launches_per_step": top["launches"] / args.steps,
+                     "ms_per_step": top["ms"] / args.steps, "share_of_step": (top["ms"] / args.steps) / ms})
 
     cpu = None
     level_cands = [s.n_candidates for s in out.stats]
@@ -331,6 +343,7 @@ def main() -> None:
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (hash-defined Bernoulli bits, on device)",
             "config": {"workload": args.workload, **spec, "method": method, "form": "batched",
+                       "tc_operands": ("e4m3" if args.tc_elem == 1 else "f16") if method == "tensor" else None,
                        "l2": "inputs (1.02 GB of bitvectors) larger than L2; no flush",
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
             "levels": [{"k": s.k, "candidates": s.n_candidates, "frequent": s.n_frequent, "ms": round(s.ms, 2)}

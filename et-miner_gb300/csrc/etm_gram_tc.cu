@@ -235,29 +235,52 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gram_tc_kernel(
 
         if (warp < 4) {
             // ---- producers ----
-            const int64_t oa = off_a[tid], ob = off_b[tid];
-            for (int64_t s = 0; s < n_stages && !*abort_flag; s++) {
-                const int64_t G = gstage + s;
-                const int slot = (int)(G % TC_STAGES);
-                const uint32_t use = (uint32_t)(G / TC_STAGES);
-                if (!mbar_wait(&empty_bar[slot], (use & 1u) ^ 1u, abort_flag)) break;
-                const int64_t w0 = s * WORDS_PER_STAGE;
-                uint64_t a0 = 0, a1 = 0, b0 = 0, b1 = 0;
-                if (oa >= 0) {
-                    a0 = __ldg(src + oa + w0);
-                    if (WORDS_PER_STAGE == 2) a1 = __ldg(src + oa + w0 + 1);
+            // Words for PF stages are loaded one batch ahead into registers, so the global
+            // latency of batch b+1 overlaps the expansion and MMAs of batch b.
+            constexpr int PF = 4;
+            constexpr int BW = PF * WORDS_PER_STAGE;  // words per row per batch (4 or 8: 16-byte aligned)
+            const int64_t oa = off_a[tid], ob = diag ? -1 : off_b[tid];
+            uint64_t cur_a[BW], cur_b[BW], nxt_a[BW], nxt_b[BW];
+            auto load_batch = [&](int64_t s0, uint64_t* xa, uint64_t* xb) {
+#pragma unroll
+                for (int q = 0; q < BW; q += 2) {
+                    ulonglong2 va = make_ulonglong2(0, 0), vb = make_ulonglong2(0, 0);
+                    if (oa >= 0) va = __ldg(reinterpret_cast<const ulonglong2*>(src + oa + s0 * WORDS_PER_STAGE + q));
+                    if (ob >= 0) vb = __ldg(reinterpret_cast<const ulonglong2*>(src + ob + s0 * WORDS_PER_STAGE + q));
+                    xa[q] = va.x;
+                    xa[q + 1] = va.y;
+                    xb[q] = vb.x;
+                    xb[q + 1] = vb.y;
                 }
-                uint8_t* slot_base = slots + slot * SLOT_BYTES;
-                store_row<ELEM>(slot_base, tid, a0, a1);
-                if (!diag) {
-                    if (ob >= 0) {
-                        b0 = __ldg(src + ob + w0);
-                        if (WORDS_PER_STAGE == 2) b1 = __ldg(src + ob + w0 + 1);
+            };
+            if (n_stages > 0) load_batch(0, cur_a, cur_b);
+            for (int64_t s0 = 0; s0 < n_stages && !*abort_flag; s0 += PF) {
+                if (s0 + PF < n_stages) load_batch(s0 + PF, nxt_a, nxt_b);
+#pragma unroll
+                for (int j = 0; j < PF; j++) {
+                    const int64_t s = s0 + j;
+                    if (s >= n_stages) break;
+                    const int64_t G = gstage + s;
+                    const int slot = (int)(G % TC_STAGES);
+                    const uint32_t use = (uint32_t)(G / TC_STAGES);
+                    if (!mbar_wait(&empty_bar[slot], (use & 1u) ^ 1u, abort_flag)) break;
+                    uint8_t* slot_base = slots + slot * SLOT_BYTES;
+                    const uint64_t a0 = cur_a[j * WORDS_PER_STAGE];
+                    const uint64_t a1 = WORDS_PER_STAGE == 2 ? cur_a[j * WORDS_PER_STAGE + 1] : 0ULL;
+                    store_row<ELEM>(slot_base, tid, a0, a1);
+                    if (!diag) {
+                        const uint64_t b0 = cur_b[j * WORDS_PER_STAGE];
+                        const uint64_t b1 = WORDS_PER_STAGE == 2 ? cur_b[j * WORDS_PER_STAGE + 1] : 0ULL;
+                        store_row<ELEM>(slot_base + ATOM_BYTES, tid, b0, b1);
                     }
-                    store_row<ELEM>(slot_base + ATOM_BYTES, tid, b0, b1);
+                    fence_proxy_async();
+                    mbar_arrive(&full_bar[slot]);
                 }
-                fence_proxy_async();
-                mbar_arrive(&full_bar[slot]);
+#pragma unroll
+                for (int q = 0; q < BW; q++) {
+                    cur_a[q] = nxt_a[q];
+                    cur_b[q] = nxt_b[q];
+                }
             }
             // ---- epilogue ----
             const bool ok = n_stages == 0 || mbar_wait(&acc_bar, tile_iter & 1u, abort_flag);

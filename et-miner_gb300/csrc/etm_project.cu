@@ -82,46 +82,60 @@ __global__ void __launch_bounds__(PT) prefix_rows_kernel(const uint64_t* __restr
     }
 }
 
-// One warp per (work entry, member): the member's column bits at the prefix's rows.
+constexpr int MB = 8;  // members per warp: the row-list loads are shared and 2 * MB gathers are in flight
+
+// One warp per (work entry, block of MB members): the members' column bits at the prefix's rows.
+// mblk_off is the exclusive prefix of ceil(m / MB) over the work entries.
 __global__ void __launch_bounds__(PT) project_kernel(const uint64_t* __restrict__ fbv, int64_t ld,
                                                      const int32_t* __restrict__ rows, int width,
                                                      const int64_t* __restrict__ grp_first,
+                                                     const int32_t* __restrict__ grp_size,
                                                      const int64_t* __restrict__ work_groups,
-                                                     const int64_t* __restrict__ mem_off, int64_t n_work,
+                                                     const int64_t* __restrict__ mblk_off, int64_t n_work,
                                                      const int64_t* __restrict__ row_off,
                                                      const int32_t* __restrict__ rowidx,
                                                      const int64_t* __restrict__ cbase, const int64_t* __restrict__ cld,
                                                      uint64_t* __restrict__ cbuf) {
     const int lane = threadIdx.x & 31;
-    const int64_t total = mem_off[n_work];
+    const int64_t total = mblk_off[n_work];
     const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < total; q += n_warps) {
-        const int64_t wi = upper_find(mem_off, n_work, q);
-        const int64_t i = q - mem_off[wi];
+        const int64_t wi = upper_find(mblk_off, n_work, q);
         const int64_t g = work_groups[wi];
-        const int64_t col = rows[(grp_first[g] + i) * width + width - 1];
-        const uint64_t* src = fbv + col * ld;
+        const int64_t m = grp_size[g];
+        const int64_t i0 = (q - mblk_off[wi]) * MB;
+        const int nm = (int)min64(MB, m - i0);
         const int32_t* R = rowidx + row_off[wi];
         const int64_t n = row_off[wi + 1] - row_off[wi];
         const int64_t stride = cld[wi];
-        uint64_t* dst = cbuf + cbase[wi] + i * stride;
+        const int64_t first = grp_first[g];
+        const uint64_t* src[MB];
+#pragma unroll
+        for (int j = 0; j < MB; j++) {
+            const int64_t col = rows[(first + i0 + (j < nm ? j : 0)) * width + width - 1];
+            src[j] = fbv + col * ld;
+        }
+        uint64_t* dst = cbuf + cbase[wi] + i0 * stride;
         const int64_t nw = (n + 63) >> 6;
         for (int64_t t = 0; t < nw; t++) {
-            const int64_t i0 = t * 64 + lane, i1 = i0 + 32;
-            int b0 = 0, b1 = 0;
-            if (i0 < n) {
-                const int32_t r = __ldg(R + i0);
-                b0 = (int)((__ldg(src + (r >> 6)) >> (r & 63)) & 1ULL);
+            const int64_t e0 = t * 64 + lane, e1 = e0 + 32;
+            const int32_t r0 = e0 < n ? __ldg(R + e0) : -1;
+            const int32_t r1 = e1 < n ? __ldg(R + e1) : -1;
+            uint64_t x0[MB], x1[MB];
+#pragma unroll
+            for (int j = 0; j < MB; j++) {
+                x0[j] = r0 >= 0 ? __ldg(src[j] + (r0 >> 6)) : 0ULL;
+                x1[j] = r1 >= 0 ? __ldg(src[j] + (r1 >> 6)) : 0ULL;
             }
-            if (i1 < n) {
-                const int32_t r = __ldg(R + i1);
-                b1 = (int)((__ldg(src + (r >> 6)) >> (r & 63)) & 1ULL);
+#pragma unroll
+            for (int j = 0; j < MB; j++) {
+                const unsigned lo = __ballot_sync(0xffffffffu, (unsigned)(x0[j] >> (r0 & 63)) & 1u);
+                const unsigned hi = __ballot_sync(0xffffffffu, (unsigned)(x1[j] >> (r1 & 63)) & 1u);
+                if (lane == j && j < nm) dst[j * stride + t] = (uint64_t)lo | ((uint64_t)hi << 32);
             }
-            const unsigned lo = __ballot_sync(0xffffffffu, b0);
-            const unsigned hi = __ballot_sync(0xffffffffu, b1);
-            if (lane == 0) dst[t] = (uint64_t)lo | ((uint64_t)hi << 32);
         }
-        for (int64_t w = nw + lane; w < stride; w += 32) dst[w] = 0ULL;
+        for (int j = 0; j < nm; j++)
+            for (int64_t w = nw + lane; w < stride; w += 32) dst[j * stride + w] = 0ULL;
     }
 }
 
@@ -154,14 +168,14 @@ extern "C" int etm_prefix_rows(const uint64_t* fbv, int64_t ld, int64_t n_words,
 }
 
 extern "C" int etm_project(const uint64_t* fbv, int64_t ld, const int32_t* rows, int32_t width,
-                           const int64_t* grp_first, const int64_t* work_groups, const int64_t* mem_off,
-                           int64_t n_work, const int64_t* row_off, const int32_t* row_idx, const int64_t* cbase,
-                           const int64_t* cld, uint64_t* cbuf, void* stream) {
+                           const int64_t* grp_first, const int32_t* grp_size, const int64_t* work_groups,
+                           const int64_t* mblk_off, int64_t n_work, const int64_t* row_off, const int32_t* row_idx,
+                           const int64_t* cbase, const int64_t* cld, uint64_t* cbuf, void* stream) {
     ETM_REQUIRE(width >= 2 && width <= 64, ETM_EINVAL, "etm_project: width %d out of range (2..64)", width);
     if (n_work <= 0) return ETM_OK;
     const int grid = max(1, sm_count()) * 8;
-    project_kernel<<<grid, PT, 0, as_stream(stream)>>>(fbv, ld, rows, width, grp_first, work_groups, mem_off, n_work,
-                                                       row_off, row_idx, cbase, cld, cbuf);
+    project_kernel<<<grid, PT, 0, as_stream(stream)>>>(fbv, ld, rows, width, grp_first, grp_size, work_groups,
+                                                       mblk_off, n_work, row_off, row_idx, cbase, cld, cbuf);
     ETM_LAUNCHED("project");
     return ETM_OK;
 }

@@ -52,7 +52,7 @@ TC_TILE = 128
 #: Largest group (rows) the tensor-core Gram counts exactly: f32 holds every integer up to 2^24.
 TC_MAX_ROWS = 1 << 24
 #: Counting method for tile-pairs: "popcount" or "tensor".
-DEFAULT_METHOD = "popcount"
+DEFAULT_METHOD = "tensor"
 
 
 def min_count(min_support: float, n_rows: int) -> int:
@@ -190,7 +190,7 @@ class Engine:
     def __init__(self, device: torch.device | int | None = None, *, method: str = DEFAULT_METHOD,
                  form: str = "batched", chunk_cands: int = CHUNK_CANDS, small_group: int = SMALL_GROUP,
                  project: bool = True, proj_density: float = PROJ_DENSITY, proj_bytes: int = PROJ_BYTES,
-                 tc_elem: int = 2):
+                 tc_elem: int = 1):
         if not torch.cuda.is_available():
             raise RuntimeError("the GB300 engine needs a CUDA device; there is no CPU fallback")
         self.lib = load_library()
@@ -304,7 +304,7 @@ class Engine:
         row_off = np.zeros(len(gids) + 1, np.int64)
         np.cumsum(cnt, out=row_off[1:])
         mem_off = np.zeros(len(gids) + 1, np.int64)
-        np.cumsum(m, out=mem_off[1:])
+        np.cumsum((m + 7) // 8, out=mem_off[1:])
         cb = np.zeros(len(gids) + 1, np.int64)
         np.cumsum(m * cl, out=cb[1:])
         tile = TC_TILE if method == 1 else TILE
@@ -324,17 +324,20 @@ class Engine:
                                                            _p(wg), n, _p(ro), _p(rowidx), _stream()))
         check(st, "etm_prefix_rows")
         st = self._launch("project", int((m * cnt).sum() * 4 // 32 + (m * cl).sum() * 8 + (m * cnt).sum() // 8),
-                          lambda: self.lib.etm_project(_p(fbv), ldp, _p(gen.rows), width, _p(grp_first), _p(wg),
-                                                       _p(mo), n, _p(ro), _p(rowidx), _p(cbase), _p(cld), _p(cbuf),
-                                                       _stream()))
+                          lambda: self.lib.etm_project(_p(fbv), ldp, _p(gen.rows), width, _p(grp_first),
+                                                       _p(grp_size), _p(wg), _p(mo), n, _p(ro), _p(rowidx),
+                                                       _p(cbase), _p(cld), _p(cbuf), _stream()))
         check(st, "etm_project")
         self._count_words(cbuf, cbase, cwords, cld, grp_size, cand_off, wg, wo, n, int(toff[-1]), base, cls, counts,
-                          method, int((m * cw).sum() * 8), float(((m.astype(np.float64) ** 2) * cw * 64).sum()))
+                          method, int((m * cw).sum() * 8), float((m * (m - 1) / 2 * cnt.astype(np.float64)).sum()))
         self.launches += 2
 
     def _count_words(self, cbuf, cbase, cwords, cld, grp_size, cand_off, wg, wo, n, n_tiles, base, cls, counts,
                      method, nbytes, macs):
-        """Tile-pair counts over member words laid out as cbuf[cbase[wi] + i * cld[wi]]: tensor or popcount."""
+        """Tile-pair counts over member words laid out as cbuf[cbase[wi] + i * cld[wi]]: tensor or popcount.
+
+        ``macs`` is the useful work: one multiply-add per candidate pair and row (sum of C(m,2) x rows).
+        """
         if method == 1:
             st = self._launch("gram_tc", nbytes, lambda: self.lib.etm_count_tiles_tc(
                 _p(cbuf), _p(cbase), _p(cwords), _p(cld), _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, n_tiles,
@@ -434,7 +437,7 @@ class Engine:
                     self._count_words(fbv, d[2 * n + 1:3 * n + 1], d[3 * n + 1:4 * n + 1], d[4 * n + 1:5 * n + 1],
                                       grp_size, cand_off, d[:n], d[n:2 * n + 1], n, int(toff[-1]), base, cls, counts,
                                       1, int(mg.sum()) * n_words * 8,
-                                      float((mg.astype(np.float64) ** 2).sum() * n_words * 64))
+                                      float((mg * (mg - 1) / 2).astype(np.float64).sum() * n_rows))
                     continue
                 if kind == "proj":
                     groups = [gids] if self.form == "batched" else [gids[q:q + 1] for q in range(len(gids))]

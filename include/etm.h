@@ -160,7 +160,8 @@ int etm_count_cands(const uint64_t* fbv, int64_t ld, int64_t n_words, const int3
  *   etm_project        member i of group wi -> cbuf[cbase[wi] + i*cld[wi] ...]:
  *                      its column's bits at the prefix rows, 64 per word, zero
  *                      padded to cld[wi] words (cld % 32 == 0, cbase even);
- *                      mem_off int64 [n_work+1] = exclusive prefix of group sizes.
+ *                      mblk_off int64 [n_work+1] = exclusive prefix of
+ *                      ceil(m/8) (one warp gathers 8 members).
  *   etm_count_tiles_proj  etm_count_tiles over the projected words
  *                      (cwords[wi] words per member; no prefix AND).
  */
@@ -171,8 +172,9 @@ int etm_prefix_rows(const uint64_t* fbv, int64_t ld, int64_t n_words, const int3
                     const int64_t* grp_first, const int64_t* work_groups, int64_t n_work, const int64_t* row_off,
                     int32_t* out_rows, void* stream);
 int etm_project(const uint64_t* fbv, int64_t ld, const int32_t* rows, int32_t width, const int64_t* grp_first,
-                const int64_t* work_groups, const int64_t* mem_off, int64_t n_work, const int64_t* row_off,
-                const int32_t* row_idx, const int64_t* cbase, const int64_t* cld, uint64_t* cbuf, void* stream);
+                const int32_t* grp_size, const int64_t* work_groups, const int64_t* mblk_off, int64_t n_work,
+                const int64_t* row_off, const int32_t* row_idx, const int64_t* cbase, const int64_t* cld,
+                uint64_t* cbuf, void* stream);
 int etm_count_tiles_proj(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                          const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
                          const int64_t* work_off, int64_t n_work, int64_t chunk_base, const uint8_t* cls,
