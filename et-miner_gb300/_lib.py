@@ -103,6 +103,7 @@ SIGNATURES: dict[str, tuple] = {
     "etm_count_tiles_tc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _P, _I32, _P, _P]),
     "etm_device_status": (ctypes.c_int, [_P]),
     "etm_level_compact": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _P, _P, _P, _I64, _I64, _I32, _P, _P, _I64, _P, _P, _I64, _P]),
+    "etm_level_compact_static": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _P, _P, _P, _I64, _I64, _I32, _P, _P, _I64, _P, _P]),
     "etm_level_subsets": (ctypes.c_int, [_P, _P, _I64, _I32, _P, _P, _I64, _P, _P, _P]),
     "etm_select_rows": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I32, _P, _P, _P, _P, _I64, _P, _P, _I64, _P]),
 }

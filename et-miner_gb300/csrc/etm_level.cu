@@ -6,6 +6,8 @@
 // Every pass is one thread per element over arrays in HBM; the compactions
 // are the three-launch ordered scans of etm_scan.cuh, so no host sort and no
 // host decode is ever needed.
+#include <mutex>
+
 #include "etm_scan.cuh"
 
 namespace {
@@ -314,6 +316,79 @@ extern "C" int etm_level_compact(const int32_t* counts, const uint8_t* cls, int6
     Survives val{counts, cls, n_cands, min_count};
     EmitSurvivor act{counts, rows, width, grp_first, grp_size, cand_off, g0, g1, out_rows, out_counts, cap};
     return scan_apply(n_cands, val, act, ws, ws_words, acc, as_stream(stream));
+}
+
+// ---- survivor compaction without caller-provided scratch ------------------------------
+//
+// etm_level_compact needs a small int64 workspace for its scan (one partial sum
+// per 4096 candidates). Some callers cannot hand one over: a serving process
+// that reserved all of its device memory up front and forbids allocations
+// once requests flow, or a host runtime that reaches this library through a
+// plain C call and owns no allocator of its own. For them the workspace lives
+// in this file, as one fixed device array per GPU.
+
+namespace {
+
+// Largest chunk the static workspace serves: 65,536 scan blocks of 4096
+// candidates, i.e. 268,435,456 candidates (the array is 512 KB + 16 bytes and
+// stays resident on every GPU that loads the library, until the process exits).
+constexpr int64_t STATIC_SCAN_BLOCKS = 65536;
+constexpr int64_t STATIC_SCAN_WORDS = STATIC_SCAN_BLOCKS + 2;
+constexpr int64_t STATIC_MAX_CANDS = STATIC_SCAN_BLOCKS * SCAN_TILE;
+constexpr int MAX_DEVICES = 64;
+
+static __device__ __align__(256) int64_t g_static_scan_ws[STATIC_SCAN_WORDS];
+
+// Device address of g_static_scan_ws, looked up once per device (with that device current).
+// On the host the symbol name is only a stand-in, never a device address.
+int64_t* static_scan_ws(int* status) {
+    static std::mutex lock;
+    static int64_t* addr[MAX_DEVICES] = {nullptr};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) {
+        set_error("etm_level_compact_static: no usable current device (%s)",
+                  e != cudaSuccess ? cudaGetErrorString(e) : "device index out of range");
+        *status = ETM_ECUDA;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> guard(lock);
+    if (addr[dev] == nullptr) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_static_scan_ws);
+        if (e != cudaSuccess || p == nullptr) {
+            set_error("etm_level_compact_static: cudaGetSymbolAddress failed on device %d: %s", dev,
+                      cudaGetErrorString(e));
+            *status = ETM_ECUDA;
+            return nullptr;
+        }
+        addr[dev] = static_cast<int64_t*>(p);
+    }
+    *status = ETM_OK;
+    return addr[dev];
+}
+
+}  // namespace
+
+extern "C" int etm_level_compact_static(const int32_t* counts, const uint8_t* cls, int64_t n_cands,
+                                        const int32_t* rows, int32_t width, const int64_t* grp_first,
+                                        const int32_t* grp_size, const int64_t* cand_off, int64_t g0, int64_t g1,
+                                        int32_t min_count, int32_t* out_rows, int32_t* out_counts, int64_t cap,
+                                        int64_t* acc, void* stream) {
+    ETM_REQUIRE(width >= 1 && width + 1 < MAXK, ETM_EINVAL, "etm_level_compact_static: width %d out of range", width);
+    ETM_REQUIRE(n_cands <= STATIC_MAX_CANDS, ETM_ENOSPACE,
+                "etm_level_compact_static: %lld candidates exceed the static workspace's limit of %lld per call; "
+                "split the chunk or use etm_level_compact with a workspace",
+                (long long)n_cands, (long long)STATIC_MAX_CANDS);
+    int status = ETM_OK;
+    int64_t* ws = static_scan_ws(&status);
+    if (status != ETM_OK) return status;
+    if (n_cands <= 0) return ETM_OK;
+    // Every call rewrites the partial sums it reads (phase 1 writes each block's sum,
+    // phase 2 the offsets), so nothing left by an earlier call needs clearing.
+    Survives val{counts, cls, n_cands, min_count};
+    EmitSurvivor act{counts, rows, width, grp_first, grp_size, cand_off, g0, g1, out_rows, out_counts, cap};
+    return scan_apply(n_cands, val, act, ws, STATIC_SCAN_WORDS, acc, as_stream(stream));
 }
 
 extern "C" int etm_level_subsets(const int32_t* new_rows, const int32_t* new_counts, int64_t n_new, int32_t width,

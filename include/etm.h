@@ -219,6 +219,25 @@ int etm_level_compact(const int32_t* counts, const uint8_t* cls, int64_t n_cands
                       int64_t cap, int64_t* acc, int64_t* ws, int64_t ws_words, void* stream);
 
 /*
+ * etm_level_compact without the workspace argument, for callers that cannot
+ * allocate device memory (a serving process that reserved its memory up front,
+ * a host runtime calling through plain C with no allocator of its own). No
+ * counterpart in the reference: its compaction always allocates through CuPy.
+ * The scan scratch is a 512 KB array compiled into the library, one per GPU,
+ * held until the process exits. Limit: n_cands <= 268,435,456 (65,536 scan
+ * blocks of 4096); larger chunks fail with ETM_ENOSPACE. The first call on a
+ * device looks up that device's array address (cudaGetSymbolAddress), so make
+ * that first call before any stream capture. All calls on a device share the
+ * array: calls that overlap on the GPU (other streams, or other host threads)
+ * race and must be serialized by the caller. Everything else (acc, cap,
+ * outputs, ordering) is as in etm_level_compact.
+ */
+int etm_level_compact_static(const int32_t* counts, const uint8_t* cls, int64_t n_cands, const int32_t* rows,
+                             int32_t width, const int64_t* grp_first, const int32_t* grp_size,
+                             const int64_t* cand_off, int64_t g0, int64_t g1, int32_t min_count, int32_t* out_rows,
+                             int32_t* out_counts, int64_t cap, int64_t* acc, void* stream);
+
+/*
  * Free flags and subset presence of a new level (k = width + 1 columns)
  * against the generating level prev (n_prev x width, with counts).
  * Replaces the free-set tests (core/cpu_miner.py:943-945, 1139-1151;
