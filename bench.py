@@ -208,6 +208,7 @@ def main() -> None:
     ap.add_argument("--method", default=None, choices=["popcount", "tensor"])
     ap.add_argument("--tc-elem", type=int, default=1, choices=[1, 2], help="tensor operands: 1 = e4m3, 2 = f16")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparator")
+    ap.add_argument("--proj-gb", type=float, default=4.0, help="device GB of projected words per chunk")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     args = ap.parse_args()
     spec = WORKLOADS[args.workload]
@@ -237,7 +238,7 @@ def main() -> None:
     method = args.method or engm.DEFAULT_METHOD
     bv = dense_k2_device(pkg, lib, spec)
     n_rows = spec["n_rows"]
-    eng = engm.Engine(form="batched", method=method, tc_elem=args.tc_elem)
+    eng = engm.Engine(form="batched", method=method, tc_elem=args.tc_elem, proj_bytes=int(args.proj_gb * (1 << 30)))
     eng.profile_kernels = True
 
     def one(e):
@@ -277,7 +278,7 @@ def main() -> None:
     # Plain form (one counting launch per prefix group): the comparator.
     plain = None
     if not args.no_plain:
-        pe = engm.Engine(form="plain", method=method, tc_elem=args.tc_elem)
+        pe = engm.Engine(form="plain", method=method, tc_elem=args.tc_elem, proj_bytes=int(args.proj_gb * (1 << 30)))
         one(pe)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
