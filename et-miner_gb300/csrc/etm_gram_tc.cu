@@ -6,21 +6,27 @@
 // of a 0/1 matrix. One CTA per SM walks tile-pairs (ti <= tj) of 128 x 128
 // members:
 //
-//   warps 0-3  producers: per stage (K = 64 transactions for f16, 128 for
-//              e4m3) each thread loads its A row's and B row's words and
-//              expands every bit into a 0.0/1.0 element, writing the 128-byte
-//              swizzled K-major operand layout the MMA reads (SWIZZLE_128B);
-//              then fence.proxy.async and an mbarrier arrive.
-//   warp 4     one thread issues tcgen05.mma (M=128, N=128) per 16/32-element
-//              K step into a TMEM f32 accumulator, and tcgen05.commit frees
-//              each stage and finally signals the epilogue.
-//   warps 0-3  epilogue: tcgen05.ld of their 32 TMEM lanes, f32 -> int32,
-//              the i < j pair counts written at their lexicographic slots.
+//   warps 0-7  producers: per stage (K = 64 transactions for f16, 128 for
+//              e4m3) thread t expands row t % 128 of A (t < 128) or of B: its
+//              words (prefetched a batch of 4 stages ahead into registers) become
+//              0.0/1.0 elements in the 128-byte swizzled K-major shared-memory
+//              layout the MMA reads (SWIZZLE_128B), then fence.proxy.async and
+//              an mbarrier arrive. Two producer warps per scheduler hide the
+//              latency of the expansion chains. (Variant A_TMEM: A rows go from
+//              registers straight into tensor memory with tcgen05.st, row i in
+//              TMEM lane i, halving the shared-memory traffic; exact too, but
+//              slower on GB300 because each stage waits for its TMEM stores.)
+//   warp 8     one thread issues tcgen05.mma (M=128, N=128; B from shared
+//              memory, A from shared memory or TMEM) per 16/32-element K step
+//              into a TMEM f32 accumulator, and tcgen05.commit frees each stage
+//              and finally signals the epilogue.
+//   warps 0-7  epilogue: tcgen05.ld of their TMEM lanes (warp % 4) and column
+//              half (warp / 4), f32 -> int32, the i < j pair counts written at
+//              their lexicographic slots.
 //
 // Exactness: every product is 0 or 1 and every partial sum is an integer
 // below 2^24 (the caller sends only groups of at most 2^24 rows here), so the
-// f32 accumulation is exact. Diagonal tile-pairs load one operand and use it
-// for both A and B.
+// f32 accumulation is exact.
 //
 // Every mbarrier wait is bounded: after WAIT_LIMIT polls the block raises an
 // abort flag, every thread leaves its loop, the MMA thread waits (bounded) for
@@ -32,15 +38,23 @@ namespace {
 
 using namespace etm;
 
-constexpr int TC_M = 128;
-constexpr int TC_N = 128;
+constexpr int TC_M = 128;  // A rows per work item
+constexpr int TC_N = 256;  // B rows per work item (a super-tile of two A tiles)
 constexpr int TC_STAGES = 4;
-constexpr int TC_PRODUCERS = 128;
+constexpr int TC_PRODUCERS = TC_M + TC_N;  // one operand row per thread: 0-127 the A rows, 128-383 the B rows
 constexpr int TC_THREADS = TC_PRODUCERS + 32;
-constexpr uint32_t TC_TMEM_COLS = 128;
-constexpr int ATOM_BYTES = 128 * 128;  // 128 rows x 128 bytes, one SWIZZLE_128B K block
-constexpr int SLOT_BYTES = 2 * ATOM_BYTES;
-constexpr int TC_SMEM_BYTES = TC_STAGES * SLOT_BYTES + 1024;
+constexpr int MMA_WARP = TC_PRODUCERS / 32;
+constexpr int EPI_WARPS = 8;                // warps 0-7 read the accumulator: lanes (w % 4), columns (w / 4)
+constexpr uint32_t TC_TMEM_COLS = 512;      // columns 0-255: the f32 accumulator; 256-383: A operand stages
+constexpr uint32_t A_TMEM_COL = 256;
+constexpr uint32_t A_STAGE_COLS = 32;       // one 128-byte operand row = 32 32-bit TMEM columns
+constexpr int A_BYTES = TC_M * 128;         // 128 rows x 128 bytes, one SWIZZLE_128B K block
+constexpr int B_BYTES = TC_N * 128;
+// Shared-memory bytes per pipeline stage: the B tile, plus the A tile unless A lives in TMEM.
+template <bool A_TMEM>
+__host__ __device__ constexpr int slot_bytes() { return A_TMEM ? B_BYTES : A_BYTES + B_BYTES; }
+template <bool A_TMEM>
+__host__ __device__ constexpr int smem_bytes() { return TC_STAGES * slot_bytes<A_TMEM>() + 1024; }
 constexpr long long WAIT_LIMIT = 1LL << 25;
 
 __device__ int g_tc_status;
@@ -65,16 +79,26 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
+// try_wait suspends the thread in hardware until the phase completes or a short time-out passes.
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
 // Waits for the phase of `parity` to complete; false if the block aborts or the wait runs out.
 __device__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
     long long n = 0;
-    while (!mbar_test(bar, parity)) {
+    while (!mbar_try(bar, parity)) {
         if (*abort_flag) return false;
         if (++n > WAIT_LIMIT) {
             *abort_flag = 1;
             return false;
         }
-        if (n > 32) __nanosleep(64);
     }
     return true;
 }
@@ -95,13 +119,14 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
 }
 
 // Instruction descriptor: D f32, A/B format code 0 (f16 for kind::f16, e4m3 for kind::f8f6f4),
-// both K-major, N = 128, M = 128.
+// both K-major, N = 256, M = 128.
 __host__ __device__ constexpr uint32_t instr_desc() {
     return (1u << 4) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
 }
 
+// D (TMEM) += A x B, both from shared-memory descriptors.
 template <int ELEM>
-__device__ __forceinline__ void mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc) {
+__device__ __forceinline__ void mma_ss(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc) {
     if constexpr (ELEM == 2) {
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -113,6 +138,49 @@ __device__ __forceinline__ void mma(uint32_t tmem_d, uint64_t a, uint64_t b, uin
             " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
             "l"(a), "l"(b), "r"(instr_desc()), "r"(acc));
     }
+}
+
+// D (TMEM) += A (TMEM, row i in lane i, K packed along columns) x B (shared memory descriptor).
+template <int ELEM>
+__device__ __forceinline__ void mma(uint32_t tmem_d, uint32_t tmem_a, uint64_t b, uint32_t acc) {
+    if constexpr (ELEM == 2) {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "r"(tmem_a), "l"(b), "r"(instr_desc()), "r"(acc));
+    } else {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "r"(tmem_a), "l"(b), "r"(instr_desc()), "r"(acc));
+    }
+}
+
+// One operand row as 32 32-bit words: bits of x0 (and x1 for e4m3) expanded to 1.0 / 0 elements.
+template <int ELEM>
+__device__ __forceinline__ void expand_row(uint64_t x0, uint64_t x1, uint32_t* w) {
+#pragma unroll
+    for (int c = 0; c < 32; c++) {
+        if constexpr (ELEM == 2) {
+            const uint32_t t = (uint32_t)(x0 >> (2 * c)) & 3u;
+            w[c] = ((t & 1u) * 0x3C00u) | ((t >> 1) * 0x3C000000u);
+        } else {
+            const uint32_t nib = (uint32_t)((c < 16 ? x0 : x1) >> (4 * (c & 15))) & 0xFu;
+            w[c] = ((nib * 0x00204081u) & 0x01010101u) * 0x38u;
+        }
+    }
+}
+
+__device__ __forceinline__ void tmem_store_row(uint32_t taddr, const uint32_t* w) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+        "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+        "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7]), "r"(w[8]),
+        "r"(w[9]), "r"(w[10]), "r"(w[11]), "r"(w[12]), "r"(w[13]), "r"(w[14]), "r"(w[15]), "r"(w[16]),
+        "r"(w[17]), "r"(w[18]), "r"(w[19]), "r"(w[20]), "r"(w[21]), "r"(w[22]), "r"(w[23]), "r"(w[24]),
+        "r"(w[25]), "r"(w[26]), "r"(w[27]), "r"(w[28]), "r"(w[29]), "r"(w[30]), "r"(w[31])
+        : "memory");
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -159,13 +227,14 @@ __device__ __forceinline__ void store_row(uint8_t* atom, int r, uint64_t x0, uin
     }
 }
 
-template <int ELEM>
+template <int ELEM, bool A_TMEM>
 __global__ void __launch_bounds__(TC_THREADS, 1) gram_tc_kernel(
     const uint64_t* __restrict__ src, const int64_t* __restrict__ cbase, const int64_t* __restrict__ cwords,
     const int64_t* __restrict__ cld, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
     const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
     const uint8_t* __restrict__ cls, int32_t* __restrict__ out) {
     constexpr int WORDS_PER_STAGE = ELEM == 2 ? 1 : 2;  // a 128-byte row holds 64 halves or 128 bytes
+    constexpr int SLOT_BYTES = slot_bytes<A_TMEM>();
     extern __shared__ uint8_t dsmem[];
     __shared__ __align__(8) uint64_t full_bar[TC_STAGES];
     __shared__ __align__(8) uint64_t empty_bar[TC_STAGES];
@@ -190,7 +259,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gram_tc_kernel(
         abort_sh = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 4) {
+    if (warp == MMA_WARP) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_sh)),
                      "r"(TC_TMEM_COLS)
                      : "memory");
@@ -207,55 +276,66 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gram_tc_kernel(
     uint32_t tile_iter = 0;  // tiles whose accumulator was committed
 
     for (int64_t tp = blockIdx.x; tp < total; tp += gridDim.x) {
+        // Work item: half h of super-tile ua (A: 128 members) against super-tile ub (B: 256 members),
+        // ua <= ub; two items per super-tile pair.
         const int64_t wi = upper_find(work_off, n_work, tp);
         const int64_t g = work_groups[wi];
         const int64_t m = grp_size[g];
-        const int64_t nt = ceil_div<int64_t>(m, TC_M);
-        int64_t ti, tj1;
-        tri_decode(tp - work_off[wi], nt + 1, &ti, &tj1);
-        const int64_t tj = tj1 - 1;
-        const bool diag = ti == tj;
+        const int64_t nb = ceil_div<int64_t>(m, TC_N);
+        const int64_t local = tp - work_off[wi];
+        int64_t ua, ub1;
+        tri_decode(local >> 1, nb + 1, &ua, &ub1);
+        const int64_t ub = ub1 - 1;
+        const int64_t a0 = ua * TC_N + (local & 1) * TC_M;  // first A member
+        const int64_t b0 = ub * TC_N;                       // first B member
+        if (a0 >= m) continue;                              // empty half (uniform across the block)
+        const bool diag = ua == ub;                         // A rows lie inside B's rows
+        const int a_in_b = (int)(local & 1);                // which half of B they are
         const int64_t cb = cand_off[g] - chunk_base;
         const int64_t words = cwords[wi];
         const int64_t n_stages = ceil_div<int64_t>(words, WORDS_PER_STAGE);
         if (tid < TC_M) {
-            const int64_t ia = ti * TC_M + tid, ib = tj * TC_N + tid;
+            const int64_t ia = a0 + tid;
             off_a[tid] = ia < m ? cbase[wi] + ia * cld[wi] : -1;
+        }
+        if (tid < TC_N) {
+            const int64_t ib = b0 + tid;
             off_b[tid] = ib < m ? cbase[wi] + ib * cld[wi] : -1;
         }
         int any = cls == nullptr;
         if (!any && tid < TC_M) {
-            const int64_t i = ti * TC_M + tid;
+            const int64_t i = a0 + tid;
             for (int c = 0; c < TC_N && !any; c++) {
-                const int64_t j = tj * TC_N + c;
+                const int64_t j = b0 + c;
                 any = i < j && j < m && cls[cb + tri_index(i, j, m)] == ETM_CAND_COUNT;
             }
         }
         if (!__syncthreads_or(any)) continue;
 
-        if (warp < 4) {
-            // ---- producers ----
+        if (warp < MMA_WARP) {
+            // ---- producers: thread t expands row t % 128 of A (t < 128) or of B ----
             // Words for PF stages are loaded one batch ahead into registers, so the global
             // latency of batch b+1 overlaps the expansion and MMAs of batch b.
             constexpr int PF = 4;
-            constexpr int BW = PF * WORDS_PER_STAGE;  // words per row per batch (4 or 8: 16-byte aligned)
-            const int64_t oa = off_a[tid], ob = diag ? -1 : off_b[tid];
-            uint64_t cur_a[BW], cur_b[BW], nxt_a[BW], nxt_b[BW];
-            auto load_batch = [&](int64_t s0, uint64_t* xa, uint64_t* xb) {
+            constexpr int BW = PF * WORDS_PER_STAGE;  // words per row per batch (16-byte aligned)
+            const bool is_b = tid >= TC_M;
+            const int prow = is_b ? tid - TC_M : tid;
+            // On a diagonal item the A rows are rows of B: the MMA reads them from B's tile.
+            const bool idle = !is_b && diag;
+            const int64_t off = idle ? -1 : (is_b ? off_b[prow] : off_a[prow]);
+            uint64_t cur[BW], nxt[BW];
+            auto load_batch = [&](int64_t s0, uint64_t* x) {
 #pragma unroll
                 for (int q = 0; q < BW; q += 2) {
-                    ulonglong2 va = make_ulonglong2(0, 0), vb = make_ulonglong2(0, 0);
-                    if (oa >= 0) va = __ldg(reinterpret_cast<const ulonglong2*>(src + oa + s0 * WORDS_PER_STAGE + q));
-                    if (ob >= 0) vb = __ldg(reinterpret_cast<const ulonglong2*>(src + ob + s0 * WORDS_PER_STAGE + q));
-                    xa[q] = va.x;
-                    xa[q + 1] = va.y;
-                    xb[q] = vb.x;
-                    xb[q + 1] = vb.y;
+                    ulonglong2 v = make_ulonglong2(0, 0);
+                    if (off >= 0) v = __ldg(reinterpret_cast<const ulonglong2*>(src + off + s0 * WORDS_PER_STAGE + q));
+                    x[q] = v.x;
+                    x[q + 1] = v.y;
                 }
             };
-            if (n_stages > 0) load_batch(0, cur_a, cur_b);
+            if (n_stages > 0) load_batch(0, cur);
             for (int64_t s0 = 0; s0 < n_stages && !*abort_flag; s0 += PF) {
-                if (s0 + PF < n_stages) load_batch(s0 + PF, nxt_a, nxt_b);
+                if (s0 + PF < n_stages) load_batch(s0 + PF, nxt);
 #pragma unroll
                 for (int j = 0; j < PF; j++) {
                     const int64_t s = s0 + j;
@@ -264,33 +344,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gram_tc_kernel(
                     const int slot = (int)(G % TC_STAGES);
                     const uint32_t use = (uint32_t)(G / TC_STAGES);
                     if (!mbar_wait(&empty_bar[slot], (use & 1u) ^ 1u, abort_flag)) break;
-                    uint8_t* slot_base = slots + slot * SLOT_BYTES;
-                    const uint64_t a0 = cur_a[j * WORDS_PER_STAGE];
-                    const uint64_t a1 = WORDS_PER_STAGE == 2 ? cur_a[j * WORDS_PER_STAGE + 1] : 0ULL;
-                    store_row<ELEM>(slot_base, tid, a0, a1);
-                    if (!diag) {
-                        const uint64_t b0 = cur_b[j * WORDS_PER_STAGE];
-                        const uint64_t b1 = WORDS_PER_STAGE == 2 ? cur_b[j * WORDS_PER_STAGE + 1] : 0ULL;
-                        store_row<ELEM>(slot_base + ATOM_BYTES, tid, b0, b1);
+                    const uint64_t x0 = cur[j * WORDS_PER_STAGE];
+                    const uint64_t x1 = WORDS_PER_STAGE == 2 ? cur[j * WORDS_PER_STAGE + 1] : 0ULL;
+                    if (idle) {
+                        // nothing to stage
+                    } else if (A_TMEM && !is_b) {
+                        // A rows go straight from registers into this warp's TMEM lanes, after the
+                        // MMAs that read this slot (their commit completed the barrier just waited on).
+                        tc_fence_after();
+                        uint32_t w[32];
+                        expand_row<ELEM>(x0, x1, w);
+                        tmem_store_row(tmem + ((uint32_t)(warp * 32) << 16) + A_TMEM_COL + slot * A_STAGE_COLS, w);
+                        tc_fence_before();
+                    } else {
+                        // Rows of the swizzled shared tiles: B (the A rows again on a diagonal
+                        // tile-pair), and A too when it does not live in TMEM.
+                        const int atom = (!A_TMEM && is_b) ? A_BYTES : 0;
+                        store_row<ELEM>(slots + slot * SLOT_BYTES + atom, prow, x0, x1);
+                        fence_proxy_async();
                     }
-                    fence_proxy_async();
                     mbar_arrive(&full_bar[slot]);
                 }
 #pragma unroll
-                for (int q = 0; q < BW; q++) {
-                    cur_a[q] = nxt_a[q];
-                    cur_b[q] = nxt_b[q];
-                }
+                for (int q = 0; q < BW; q++) cur[q] = nxt[q];
             }
-            // ---- epilogue ----
+            // ---- epilogue: warp w < 8 reads TMEM lanes 32 (w % 4) .. +31, columns 128 (w / 4) .. +127 ----
             const bool ok = n_stages == 0 || mbar_wait(&acc_bar, tile_iter & 1u, abort_flag);
-            if (ok) {
+            if (ok && warp < EPI_WARPS) {
                 tc_fence_after();
-                const int64_t i = ti * TC_M + warp * 32 + lane;
-                for (int q = 0; q < TC_N / 32; q++) {
+                const int lane_base = (warp & 3) * 32;
+                const int64_t i = a0 + lane_base + lane;
+                for (int q = 0; q < 4; q++) {
+                    const int col0 = (warp >> 2) * 128 + q * 32;
                     uint32_t v[32];
                     if (n_stages > 0) {
-                        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(q * 32);
+                        const uint32_t taddr = tmem + ((uint32_t)lane_base << 16) + (uint32_t)col0;
                         asm volatile(
                             "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
                             "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -308,7 +396,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gram_tc_kernel(
                     if (i < m) {
 #pragma unroll
                         for (int c = 0; c < 32; c++) {
-                            const int64_t j = tj * TC_N + q * 32 + c;
+                            const int64_t j = b0 + col0 + c;
                             if (i < j && j < m) {
                                 const int64_t t = cb + tri_index(i, j, m);
                                 if (cls == nullptr || cls[t] == ETM_CAND_COUNT)
@@ -328,11 +416,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gram_tc_kernel(
                 const uint32_t use = (uint32_t)(G / TC_STAGES);
                 if (!mbar_wait(&full_bar[slot], use & 1u, abort_flag)) break;
                 tc_fence_after();
-                const uint32_t a_addr = smem_u32(slots + slot * SLOT_BYTES);
-                const uint32_t b_addr = diag ? a_addr : a_addr + ATOM_BYTES;
+                const uint32_t base = smem_u32(slots + slot * SLOT_BYTES);
+                const uint32_t b_addr = A_TMEM ? base : base + A_BYTES;
+                // A: its own tile, or on a diagonal item rows 128 h.. of B's tile (16 KB per 128 rows).
+                const uint32_t a_addr = diag ? b_addr + a_in_b * A_BYTES : base;
+                const uint32_t a_tmem = tmem + A_TMEM_COL + slot * A_STAGE_COLS;
 #pragma unroll
-                for (int k = 0; k < 4; k++) {  // 4 x 32 bytes of K per 128-byte row
-                    mma<ELEM>(tmem, smem_desc(a_addr + 32 * k), smem_desc(b_addr + 32 * k), (s > 0 || k > 0) ? 1u : 0u);
+                for (int k = 0; k < 4; k++) {  // 4 x 32 bytes of K per 128-byte row (8 TMEM columns of A)
+                    const uint32_t acc = (s > 0 || k > 0) ? 1u : 0u;
+                    if (A_TMEM && !diag) mma<ELEM>(tmem, a_tmem + 8 * k, smem_desc(b_addr + 32 * k), acc);
+                    else mma_ss<ELEM>(tmem, smem_desc(a_addr + 32 * k), smem_desc(b_addr + 32 * k), acc);
                 }
                 mma_commit(&empty_bar[slot]);
             }
@@ -345,7 +438,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gram_tc_kernel(
     }
 
     // Teardown: make sure no MMA is still writing TMEM, then free it.
-    if (warp == 4) {
+    if (warp == MMA_WARP) {
         if (lane == 0 && *abort_flag) {
             mma_commit(&drain_bar);
             long long n = 0;
@@ -358,21 +451,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gram_tc_kernel(
     if (tid == 0 && *abort_flag) atomicExch(&g_tc_status, ETM_ETIMEOUT);
 }
 
-template <int ELEM>
+template <int ELEM, bool A_TMEM>
 int launch_gram(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                 const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
                 int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t* out,
                 cudaStream_t s) {
     static bool configured = false;
     if (!configured) {
-        ETM_CUDA(cudaFuncSetAttribute(gram_tc_kernel<ELEM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      TC_SMEM_BYTES));
+        ETM_CUDA(cudaFuncSetAttribute(gram_tc_kernel<ELEM, A_TMEM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      smem_bytes<A_TMEM>()));
         configured = true;
     }
     const int64_t sms = max(1, sm_count());
     const int grid = (int)max64(1, min64(sms, n_tiles > 0 ? n_tiles : sms));
-    gram_tc_kernel<ELEM><<<grid, TC_THREADS, TC_SMEM_BYTES, s>>>(cbuf, cbase, cwords, cld, grp_size, cand_off,
-                                                                 work_groups, work_off, n_work, chunk_base, cls, out);
+    gram_tc_kernel<ELEM, A_TMEM><<<grid, TC_THREADS, smem_bytes<A_TMEM>(), s>>>(
+        cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, chunk_base, cls, out);
     ETM_LAUNCHED("gram_tc");
     return ETM_OK;
 }
@@ -385,12 +478,15 @@ int gram_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, c
             const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
             int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t elem, int32_t* out,
             cudaStream_t s) {
-    if (elem == 2)
-        return launch_gram<2>(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, n_tiles,
-                              chunk_base, cls, out, s);
-    ETM_REQUIRE(elem == 1, ETM_EINVAL, "gram_tc: element size %d (1 = e4m3, 2 = f16)", elem);
-    return launch_gram<1>(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, n_tiles,
-                          chunk_base, cls, out, s);
+    // elem: 1 = e4m3, 2 = f16; + ETM_TC_A_TMEM: the A operand is staged in tensor memory
+    // (tcgen05.st) instead of shared memory.
+    const bool a_tmem = (elem & ETM_TC_A_TMEM) != 0;
+    const int e = elem & ~ETM_TC_A_TMEM;
+    ETM_REQUIRE(e == 1 || e == 2, ETM_EINVAL, "gram_tc: element code %d (1 = e4m3, 2 = f16)", e);
+#define ETM_GRAM_ARGS cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, n_tiles, chunk_base, cls, out, s
+    if (e == 2) return a_tmem ? launch_gram<2, true>(ETM_GRAM_ARGS) : launch_gram<2, false>(ETM_GRAM_ARGS);
+    return a_tmem ? launch_gram<1, true>(ETM_GRAM_ARGS) : launch_gram<1, false>(ETM_GRAM_ARGS);
+#undef ETM_GRAM_ARGS
 }
 
 int count_tiles_tensor(const uint64_t*, int64_t, int64_t, const int32_t*, int32_t, const int64_t*, const int32_t*,

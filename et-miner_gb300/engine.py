@@ -47,8 +47,9 @@ CHUNK_CANDS = 1 << 27
 PROJ_DENSITY = 0.5
 #: Device bytes of projected suffix words (and row lists) per chunk.
 PROJ_BYTES = 4 << 30
-#: Members per tile side of the tensor-core Gram kernel.
-TC_TILE = 128
+#: Members per B super-tile of the tensor-core Gram kernel; each super-tile pair (ua <= ub) is two
+#: work items (the two 128-member halves of ua against all 256 members of ub).
+TC_TILE = 256
 #: Largest group (rows) the tensor-core Gram counts exactly: f32 holds every integer up to 2^24.
 TC_MAX_ROWS = 1 << 24
 #: Counting method for tile-pairs: "popcount" or "tensor".
@@ -64,6 +65,15 @@ def mining_min_count(min_support: float, n_rows: int) -> int:
     """The threshold the levels apply: ``min_count``, at least 1, as the CPU route does
     (core/cpu_miner.py:967-970); at 0 every pair would be "frequent" with count 0."""
     return max(1, min_count(min_support, n_rows))
+
+
+def _tile_items(m: np.ndarray, method: int) -> np.ndarray:
+    """Work items of groups of m members: 64 x 64 tile-pairs (popcount) or 128 x 256 Gram items (tensor)."""
+    if method == 1:
+        nb = (m + TC_TILE - 1) // TC_TILE
+        return nb * (nb + 1)
+    nt = (m + TILE - 1) // TILE
+    return nt * (nt + 1) // 2
 
 
 def _p(t: torch.Tensor | None) -> int | None:
@@ -307,10 +317,8 @@ class Engine:
         np.cumsum((m + 7) // 8, out=mem_off[1:])
         cb = np.zeros(len(gids) + 1, np.int64)
         np.cumsum(m * cl, out=cb[1:])
-        tile = TC_TILE if method == 1 else TILE
-        nt = (m + tile - 1) // tile
         toff = np.zeros(len(gids) + 1, np.int64)
-        np.cumsum(nt * (nt + 1) // 2, out=toff[1:])
+        np.cumsum(_tile_items(m, method), out=toff[1:])
         n = len(gids)
         host = np.concatenate([gids.astype(np.int64), toff, row_off, mem_off, cb[:-1], cw, cl])
         d = torch.from_numpy(host).to(self.device)
@@ -427,9 +435,8 @@ class Engine:
                     continue
                 if kind == "tiles" and whole_tc:
                     mg = sizes[gids]
-                    nt = (mg + TC_TILE - 1) // TC_TILE
                     toff = np.zeros(len(gids) + 1, np.int64)
-                    np.cumsum(nt * (nt + 1) // 2, out=toff[1:])
+                    np.cumsum(_tile_items(mg, 1), out=toff[1:])
                     n = len(gids)
                     host = np.concatenate([gids, toff, np.zeros(n, np.int64), np.full(n, n_words, np.int64),
                                            np.full(n, ldp, np.int64)])

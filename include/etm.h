@@ -51,6 +51,10 @@ extern "C" {
 #define ETM_METHOD_POPCOUNT 0 /* AND + popcount on CUDA cores */
 #define ETM_METHOD_TENSOR 1   /* 0/1 Gram on tcgen05 tensor cores, f32 accumulation in TMEM, exact */
 
+/* Flag added to etm_count_tiles_tc's elem: stage the A operand in tensor memory (tcgen05.st)
+ * instead of shared memory. Exact either way; the shared-memory form is faster on GB300. */
+#define ETM_TC_A_TMEM 4
+
 int etm_version(void);
 /* Message of the last failing call on this thread (empty if none). */
 const char* etm_last_error(void);
@@ -182,13 +186,15 @@ int etm_count_tiles_proj(const uint64_t* cbuf, const int64_t* cbase, const int64
 
 /*
  * etm_count_tiles_proj on the tcgen05 tensor cores: the pair counts of each
- * listed group are the Gram matrix of its 0/1 member words, computed by
- * 128 x 128 tile-pairs with bits expanded in shared memory to f16 (elem 2,
- * kind::f16) or e4m3 (elem 1, kind::f8f6f4) and f32 accumulation in TMEM.
- * Exact while every group has at most 2^24 rows (cwords <= 262144): the caller
- * sends larger groups to the popcount kernels. work_off counts tile-pairs of
- * 128 members: T(T+1)/2, T = ceil(m/128); n_tiles = work_off[n_work] (sizes
- * the grid). New in this engine (the reference counts on CUDA cores only).
+ * listed group are the Gram matrix of its 0/1 member words, computed in work
+ * items of 128 x 256 members (M = 128, N = 256) with bits expanded in shared
+ * memory to f16 (elem 2, kind::f16) or e4m3 (elem 1, kind::f8f6f4) and f32
+ * accumulation in TMEM. Exact while every group has at most 2^24 rows
+ * (cwords <= 262144): the caller sends larger groups to the popcount kernels.
+ * work_off counts work items: nb(nb+1) per group, nb = ceil(m/256) (the two
+ * 128-member halves of super-tile ua against super-tile ub, ua <= ub);
+ * n_tiles = work_off[n_work] (sizes the grid). New in this engine (the
+ * reference counts on CUDA cores only).
  */
 int etm_count_tiles_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                        const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,

@@ -36,8 +36,9 @@ def _k2(pkg, bv_np, method, elem=2):
     return new.rows.cpu().numpy(), new.counts.cpu().numpy()
 
 
-@pytest.mark.parametrize("elem", [2, 1])
-@pytest.mark.parametrize("n_f,n_words", [(2, 1), (127, 31), (128, 32), (129, 33), (300, 65), (257, 3)])
+@pytest.mark.parametrize("elem", [2, 1, 2 | 4, 1 | 4])  # 4: A operand staged in tensor memory
+@pytest.mark.parametrize("n_f,n_words", [(2, 1), (127, 31), (128, 32), (129, 33), (255, 4), (256, 5), (257, 3),
+                                         (300, 65), (513, 6)])
 def test_pair_counts_match_popcount(pkg, n_f, n_words, elem):
     rng = np.random.default_rng(n_f * 1000 + n_words)
     bv = rng.integers(0, 2**63, size=(n_f, n_words), dtype=np.int64).view(np.uint64)
