@@ -189,6 +189,71 @@ def run_reference(args, spec) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_serving(args) -> None:
+    """Serving workload: 256 Poisson-arriving requests over 8 resident datasets, p50/p99 latency."""
+    import torch
+
+    from oracle import miner
+
+    pkg = _pkg()
+    pkg.build_library()
+    from importlib import import_module
+
+    serve = import_module(pkg.__name__ + ".serve")
+    engm = import_module(pkg.__name__ + ".engine")
+    syn = pkg.synthetic
+    t0 = time.perf_counter()
+    raw = syn.serving_datasets(seed=0, scale=args.serving_scale)
+    datasets = [serve.dataset_from_transactions(t.indptr, t.items) for t, _ in raw]
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    reqs = syn.serving_requests(args.serving_requests, mean_gap_s=0.05, seed=0)
+    # Warm-up: one small request per dataset (library load, first launches).
+    with serve.Server(datasets, slots=args.slots) as server:
+        for f in [server.submit(d, 0.05, 2) for d in range(len(datasets))]:
+            f.result()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    with serve.Server(datasets, slots=args.slots) as server:
+        t1 = time.perf_counter()
+        futs = serve.replay(server, reqs)
+        results = [f.result() for f in futs]
+        makespan = time.perf_counter() - t1
+        st = server.stats()
+    clk = clocks.stop()
+    # Exactness: sampled requests against the same request mined alone, and the CPU oracle on small datasets.
+    rng = np.random.default_rng(0)
+    sample = rng.choice(len(reqs), size=min(16, len(reqs)), replace=False)
+    alone_ok = oracle_ok = 0
+    oracle_n = 0
+    for i in sample:
+        r, res = reqs[i], results[i]
+        ds = datasets[r.dataset]
+        alone = engm.Engine(chunk_cands=1 << 24, proj_bytes=1 << 30).mine(ds.bitvecs, ds.n_rows, r.min_support,
+                                                                          r.max_length)
+        a_levels = [(ds.items[c], n) for c, n in alone.host_levels()]
+        got = miner.canonical(res.levels)
+        alone_ok += int(got == miner.canonical(a_levels))
+        if ds.n_rows <= 60_000 and oracle_n < 6:
+            t = raw[r.dataset][0]
+            ref, items = miner.mine_transactions(t.indptr, t.items, t.n_rows, r.min_support, r.max_length)
+            oracle_ok += int(got == miner.canonical(ref.levels, items))
+            oracle_n += 1
+    line = {
+        "metric": "serving p99 latency, 256 Poisson requests (mean gap 50 ms) over 8 resident datasets",
+        "value": st["p99_s"], "unit": "s", "n_gpus": 1, "steps": 1, "warmup": len(datasets),
+        "ms_per_step": makespan * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64", "data": "synthetic (seeded serving datasets and request stream)",
+        "config": {"workload": "serving", "requests": len(reqs), "slots": args.slots, "scale": args.serving_scale,
+                   "datasets": [{"rows": ds.n_rows, "items": ds.n_cols} for ds in datasets]},
+        "p50_s": st["p50_s"], "p99_s": st["p99_s"], "mean_s": st["mean_s"], "max_s": st["max_s"],
+        "queued_p99_s": st["queued_p99_s"], "throughput_rps": len(reqs) / makespan, "makespan_s": makespan,
+        "dataset_build_s": build_s,
+        "exact": {"alone_equal": f"{alone_ok}/{len(sample)}", "oracle_equal": f"{oracle_ok}/{oracle_n}"},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def _pkg():
     import __graft_entry__ as g
 
@@ -204,13 +269,23 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="dense_k2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="dense_k2", choices=sorted(WORKLOADS) + ["serving"])
+    ap.add_argument("--slots", type=int, default=4, help="serving: requests on the GPU at once")
+    ap.add_argument("--serving-scale", type=float, default=1.0, help="serving: dataset row scale")
+    ap.add_argument("--serving-requests", type=int, default=256)
     ap.add_argument("--method", default=None, choices=["popcount", "tensor"])
     ap.add_argument("--tc-elem", type=int, default=1, choices=[1, 2], help="tensor operands: 1 = e4m3, 2 = f16")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparator")
     ap.add_argument("--proj-gb", type=float, default=4.0, help="device GB of projected words per chunk")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     args = ap.parse_args()
+    if args.workload == "serving":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the serving workload has no CPU arm"}))
+            return
+        if int(os.environ.get("RANK", "0")) == 0:
+            run_serving(args)
+        return
     spec = WORKLOADS[args.workload]
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -200,7 +200,7 @@ class Engine:
     def __init__(self, device: torch.device | int | None = None, *, method: str = DEFAULT_METHOD,
                  form: str = "batched", chunk_cands: int = CHUNK_CANDS, small_group: int = SMALL_GROUP,
                  project: bool = True, proj_density: float = PROJ_DENSITY, proj_bytes: int = PROJ_BYTES,
-                 tc_elem: int = 1):
+                 tc_elem: int = 1, pipeline: bool = True):
         if not torch.cuda.is_available():
             raise RuntimeError("the GB300 engine needs a CUDA device; there is no CPU fallback")
         self.lib = load_library()
@@ -219,12 +219,20 @@ class Engine:
         self.proj_bytes = int(proj_bytes)
         #: Tensor-core operand element: 2 = f16 (kind::f16), 1 = e4m3 (kind::f8f6f4).
         self.tc_elem = int(tc_elem)
+        #: Batched form: project chunk c+1 on a side stream while chunk c is counted.
+        self.pipeline = bool(pipeline)
         self.scratch = _Scratch(self.device)
         self.launches = 0
         #: When set, every counting / compaction launch is bracketed by CUDA events on its stream.
         self.profile_kernels = False
         self._events: list[tuple] = []
         self.used_tensor = False
+
+    def _side_stream(self) -> torch.cuda.Stream:
+        """The stream projection runs on beside the counting kernels (created on first use)."""
+        if getattr(self, "_side", None) is None:
+            self._side = torch.cuda.Stream(device=self.device)
+        return self._side
 
     # -- kernel timing ----------------------------------------------------------
     def _launch(self, name: str, nbytes: int, fn, flops: float = 0.0):
@@ -303,9 +311,12 @@ class Engine:
         self.launches += 1
         return out.cpu().numpy().copy()
 
-    def _count_projected(self, fbv, ldp, n_words, gen, grp_first, grp_size, cand_off, gids, sizes, pcnt, base, cls,
-                         counts, method):
-        """Row lists, projected suffix words and tile-pair counts of the listed groups (one launch each)."""
+    def _prep_projected(self, fbv, ldp, n_words, gen, grp_first, grp_size, gids, sizes, pcnt, method, buf: int = 0):
+        """Row lists and projected member words of the listed groups (two launches on the current stream).
+
+        Returns what ``_count_prepped`` needs. ``buf`` selects one of two scratch sets, so the
+        projection of the next chunk can run while the current one is counted.
+        """
         width = gen.k
         m = sizes[gids]
         cnt = pcnt[gids]
@@ -325,8 +336,8 @@ class Engine:
         wg, wo = d[:n], d[n:2 * n + 1]
         ro, mo = d[2 * n + 1:3 * n + 2], d[3 * n + 2:4 * n + 3]
         cbase, cwords, cld = d[4 * n + 3:5 * n + 3], d[5 * n + 3:6 * n + 3], d[6 * n + 3:7 * n + 3]
-        rowidx = self.scratch.get("proj_rows", int(row_off[-1]), torch.int32)
-        cbuf = self.scratch.get("proj_cbuf", int(cb[-1]), torch.int64)
+        rowidx = self.scratch.get(f"proj_rows_{buf}", int(row_off[-1]), torch.int32)
+        cbuf = self.scratch.get(f"proj_cbuf_{buf}", int(cb[-1]), torch.int64)
         st = self._launch("prefix_rows", int(n * (width - 1) * n_words * 8 + row_off[-1] * 4),
                           lambda: self.lib.etm_prefix_rows(_p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first),
                                                            _p(wg), n, _p(ro), _p(rowidx), _stream()))
@@ -336,9 +347,22 @@ class Engine:
                                                        _p(grp_size), _p(wg), _p(mo), n, _p(ro), _p(rowidx),
                                                        _p(cbase), _p(cld), _p(cbuf), _stream()))
         check(st, "etm_project")
-        self._count_words(cbuf, cbase, cwords, cld, grp_size, cand_off, wg, wo, n, int(toff[-1]), base, cls, counts,
-                          method, int((m * cw).sum() * 8), float((m * (m - 1) / 2 * cnt.astype(np.float64)).sum()))
         self.launches += 2
+        return dict(d=d, cbuf=cbuf, cbase=cbase, cwords=cwords, cld=cld, wg=wg, wo=wo, n=n, n_tiles=int(toff[-1]),
+                    nbytes=int((m * cw).sum() * 8), macs=float((m * (m - 1) / 2 * cnt.astype(np.float64)).sum()))
+
+    def _count_prepped(self, prep, grp_size, cand_off, base, cls, counts, method):
+        """The tile-pair counts of a prepared projection (one launch on the current stream)."""
+        prep["d"].record_stream(torch.cuda.current_stream())
+        self._count_words(prep["cbuf"], prep["cbase"], prep["cwords"], prep["cld"], grp_size, cand_off, prep["wg"],
+                          prep["wo"], prep["n"], prep["n_tiles"], base, cls, counts, method, prep["nbytes"],
+                          prep["macs"])
+
+    def _count_projected(self, fbv, ldp, n_words, gen, grp_first, grp_size, cand_off, gids, sizes, pcnt, base, cls,
+                         counts, method):
+        """Row lists, projected suffix words and tile-pair counts of the listed groups (one launch each)."""
+        prep = self._prep_projected(fbv, ldp, n_words, gen, grp_first, grp_size, gids, sizes, pcnt, method)
+        self._count_prepped(prep, grp_size, cand_off, base, cls, counts, method)
 
     def _count_words(self, cbuf, cbase, cwords, cld, grp_size, cand_off, wg, wo, n, n_tiles, base, cls, counts,
                      method, nbytes, macs):
@@ -410,12 +434,46 @@ class Engine:
         method = 1 if tensor else 0
         # K=2 on the tensor cores: the one group of every generator, its members the padded columns.
         whole_tc = tensor and width == 1 and n_rows <= TC_MAX_ROWS
+        # Chunks: whole groups within both budgets (at least one group each).
+        chunks = []
         g0 = 0
         while g0 < G:
-            # Chunk: whole groups within both budgets (at least one group).
             g1c = int(np.searchsorted(offs, offs[g0] + self.chunk_cands, side="right")) - 1
             g1p = int(np.searchsorted(pcum, pcum[g0] + self.proj_bytes, side="right")) - 1
             g1 = max(min(g1c, g1p), g0 + 1)
+            chunks.append((g0, g1))
+            g0 = g1
+        # Batched form: the projection of chunk c+1 runs on a side stream while chunk c is counted
+        # (memory-bound gathers beside tensor-bound MMAs); two scratch sets alternate.
+        pipelined = self.pipeline and self.form == "batched" and proj.any()
+        main = torch.cuda.current_stream()
+        side = self._side_stream() if pipelined else None
+        prep_done = [torch.cuda.Event(), torch.cuda.Event()]
+        buf_free = [torch.cuda.Event(), torch.cuda.Event()]
+        preps: dict[int, dict] = {}
+
+        def proj_ids(c):
+            a, b = chunks[c]
+            sel = proj[a:b] & (sizes[a:b] > self.small_group)
+            return np.arange(a, b, dtype=np.int64)[sel]
+
+        def prep(c):
+            ids_c = proj_ids(c)
+            if len(ids_c) == 0:
+                return
+            buf = c % 2
+            with torch.cuda.stream(side):
+                side.wait_event(buf_free[buf])
+                preps[c] = self._prep_projected(fbv, ldp, n_words, gen, grp_first, grp_size, ids_c, sizes, pcnt,
+                                                method, buf)
+                prep_done[buf].record(side)
+
+        if pipelined:
+            start_ev = torch.cuda.Event()
+            start_ev.record(main)
+            side.wait_event(start_ev)  # the generating level and group tables come from the main stream
+            prep(0)
+        for c, (g0, g1) in enumerate(chunks):
             base = int(offs[g0])
             n_c = int(offs[g1] - base)
             counts = self.scratch.get("chunk_counts", n_c, torch.int32)
@@ -429,9 +487,20 @@ class Engine:
             ids = np.arange(g0, g1, dtype=np.int64)
             small = m <= self.small_group
             pr = proj[g0:g1]
-            for kind, sel in (("cands", small), ("tiles", ~small & ~pr), ("proj", pr)):
+            for kind, sel in (("cands", small), ("tiles", ~small & ~pr), ("proj", pr & ~small)):
                 gids = ids[sel]
                 if len(gids) == 0:
+                    continue
+                if kind == "proj":
+                    if pipelined:
+                        main.wait_event(prep_done[c % 2])
+                        self._count_prepped(preps.pop(c), grp_size, cand_off, base, cls, counts, method)
+                        buf_free[c % 2].record(main)
+                        continue
+                    groups = [gids] if self.form == "batched" else [gids[q:q + 1] for q in range(len(gids))]
+                    for bg in groups:
+                        self._count_projected(fbv, ldp, n_words, gen, grp_first, grp_size, cand_off, bg, sizes, pcnt,
+                                              base, cls, counts, method)
                     continue
                 if kind == "tiles" and whole_tc:
                     mg = sizes[gids]
@@ -445,12 +514,6 @@ class Engine:
                                       grp_size, cand_off, d[:n], d[n:2 * n + 1], n, int(toff[-1]), base, cls, counts,
                                       1, int(mg.sum()) * n_words * 8,
                                       float((mg * (mg - 1) / 2).astype(np.float64).sum() * n_rows))
-                    continue
-                if kind == "proj":
-                    groups = [gids] if self.form == "batched" else [gids[q:q + 1] for q in range(len(gids))]
-                    for bg in groups:
-                        self._count_projected(fbv, ldp, n_words, gen, grp_first, grp_size, cand_off, bg, sizes, pcnt,
-                                              base, cls, counts, method)
                     continue
                 if kind == "cands":
                     w = m[sel] * (m[sel] - 1) // 2
@@ -475,6 +538,8 @@ class Engine:
                             _p(wg), _p(wo), len(bg), base, _p(cls), method, _p(counts), _stream()))
                     check(st, f"etm_count_{kind}")
                     self.launches += 1
+            if pipelined and c + 1 < len(chunks):
+                prep(c + 1)  # overlaps this chunk's counting and the host wait in its compaction
             ws = self.scratch.get("ws_compact", scan_words(n_c), torch.int64)
             while True:
                 st = self._launch("level_compact", n_c * (5 if classify else 4), lambda: self.lib.etm_level_compact(
@@ -494,7 +559,6 @@ class Engine:
                 acc.fill_(n_out)
             n_out = new_total
             stats.n_chunks += 1
-            g0 = g1
         if self.used_tensor:
             st = self.lib.etm_device_status(_stream())
             if st != 0:
@@ -585,5 +649,5 @@ class Engine:
 def mine(bitvecs, n_rows: int, min_support: float, max_length: int | None = None, **kw) -> MineOutput:
     """Mine device bitvectors [n_cols, ceil(N/64)] with a fresh ``Engine`` (see ``Engine.mine``)."""
     engine_kw = {k: kw.pop(k) for k in ("method", "form", "chunk_cands", "small_group", "device", "project",
-                                        "proj_density", "proj_bytes", "tc_elem") if k in kw}
+                                        "proj_density", "proj_bytes", "tc_elem", "pipeline") if k in kw}
     return Engine(**engine_kw).mine(bitvecs, n_rows, min_support, max_length, **kw)
