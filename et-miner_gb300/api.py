@@ -210,8 +210,12 @@ def _frequent_csr(indptr: np.ndarray, flat: np.ndarray, n_rows: int, mc: int):
     return row_ptr, cols, items[keep]
 
 
-def build_device_bitvecs(row_ptr: np.ndarray, cols: np.ndarray, n_cols: int, n_rows: int, device=None):
-    """Column bitvectors [n_cols, ceil(N/64)] (torch int64 view of uint64) built on the device by etm_build_bitvecs."""
+def build_device_bitvecs(row_ptr: np.ndarray, cols: np.ndarray, n_cols: int, n_rows: int, device=None,
+                         keep_rows: bool = False):
+    """Column bitvectors [n_cols, ceil(N/64)] (torch int64 view of uint64) built on the device by etm_build_bitvecs.
+
+    With ``keep_rows`` also returns the device CSR (row_ptr, cols) and the host row lengths, for the
+    row-wise K=2 kernel."""
     import torch
 
     from ._lib import check, load_library
@@ -226,6 +230,8 @@ def build_device_bitvecs(row_ptr: np.ndarray, cols: np.ndarray, n_cols: int, n_r
         raise ValueError("row_ptr must be a non-decreasing [n_rows + 1] array ending at len(cols)")
     check(lib.etm_build_bitvecs(rp.data_ptr(), ids.data_ptr(), len(cols), None, 0, n_rows, n_cols, ld, bv.data_ptr(),
                                 torch.cuda.current_stream().cuda_stream), "etm_build_bitvecs")
+    if keep_rows:
+        return bv[:n_cols], (rp, ids, np.diff(row_ptr))
     return bv[:n_cols]
 
 
@@ -449,11 +455,11 @@ def apriori(
     if len(items) == 0:
         df = _frame([], max(1, n_rows), wide)
         return (df, session) if profile else df
-    bv = build_device_bitvecs(row_ptr, cols, len(items), n_rows)
+    bv, rows = build_device_bitvecs(row_ptr, cols, len(items), n_rows, keep_rows=True)
     max_tx = int(np.diff(indptr).max()) if n_rows else 0
     eff = min(max_length, max_tx) if max_length else max_tx
     out = eng.mine(bv, n_rows, min_support, eff if eff >= 1 else 1, prune_equal_support=prune_equal_support,
-                   use_generator_pruning=use_generator_pruning, level_callback=level_callback)
+                   use_generator_pruning=use_generator_pruning, level_callback=level_callback, rows=rows)
     if warn_complexity and out.stats:
         _warn_complexity(out.stats[0].n_frequent, min_support)
     df = _emit(out, items.astype(np.uint64 if wide else np.int64))

@@ -35,6 +35,7 @@ import torch
 
 from . import _lib
 from ._lib import check, load_library
+from .autotune import Autotuner
 
 #: A prefix group with at most this many members is counted one warp per candidate.
 SMALL_GROUP = 16
@@ -52,6 +53,8 @@ PROJ_BYTES = 4 << 30
 TC_TILE = 256
 #: Largest group (rows) the tensor-core Gram counts exactly: f32 holds every integer up to 2^24.
 TC_MAX_ROWS = 1 << 24
+#: Row-wise K=2 crossover: rows' pair increments over pairs x words (the reference's K2_ROWS_MAX_R).
+K2_ROWS_MAX_R = 3.95e-3
 #: Counting method for tile-pairs: "popcount" or "tensor".
 DEFAULT_METHOD = "tensor"
 
@@ -200,7 +203,7 @@ class Engine:
     def __init__(self, device: torch.device | int | None = None, *, method: str = DEFAULT_METHOD,
                  form: str = "batched", chunk_cands: int = CHUNK_CANDS, small_group: int = SMALL_GROUP,
                  project: bool = True, proj_density: float = PROJ_DENSITY, proj_bytes: int = PROJ_BYTES,
-                 tc_elem: int = 1, pipeline: bool = True):
+                 tc_elem: int = 1, pipeline: bool = True, autotune: "Autotuner | bool | None" = None):
         if not torch.cuda.is_available():
             raise RuntimeError("the GB300 engine needs a CUDA device; there is no CPU fallback")
         self.lib = load_library()
@@ -221,6 +224,12 @@ class Engine:
         self.tc_elem = int(tc_elem)
         #: Batched form: project chunk c+1 on a side stream while chunk c is counted.
         self.pipeline = bool(pipeline)
+        #: K=2 counts row-wise from the transactions (when given) while
+        #: sum C(len,2) / (pairs x words) is below this (gpu/row_split_chunks.py:130-142); 0 disables.
+        self.k2_rows_max_r = K2_ROWS_MAX_R
+        self._k2_rows = None
+        #: Counting settings chosen per level shape by timing (None: the fixed defaults).
+        self.autotuner = Autotuner() if autotune is True else (autotune or None)
         self.scratch = _Scratch(self.device)
         self.launches = 0
         #: When set, every counting / compaction launch is bracketed by CUDA events on its stream.
@@ -399,13 +408,65 @@ class Engine:
         n_rows = n_words * 64 if n_rows is None else n_rows
         G, total, grp_first, grp_size, cand_off = self.groups(gen)
         stats = LevelStats(width + 1, total, 0, 0.0, G)
-        out_rows = torch.empty((0, width + 1), dtype=torch.int32, device=self.device)
-        out_counts = torch.empty(0, dtype=torch.int32, device=self.device)
         if total == 0:
             stats.ms = (time.perf_counter() - t0) * 1e3
-            return Level(out_rows, out_counts), stats
+            empty = Level(torch.empty((0, width + 1), dtype=torch.int32, device=self.device),
+                          torch.empty(0, dtype=torch.int32, device=self.device))
+            return empty, stats
         sizes = grp_size[:G].cpu().numpy().astype(np.int64)
         offs = cand_off[: G + 1].cpu().numpy()
+        args = (gen, fbv, ldp, n_words, mc, infer, prune, n_rows, G, total, grp_first, grp_size, cand_off, sizes,
+                offs, stats)
+        tuner = self.autotuner
+        if tuner is None or total < tuner.min_candidates:
+            level = self._count_groups(*args)
+        else:
+            key = tuner.key(width + 1, n_words, sizes, total, self.method)
+            if key in tuner.cache:
+                with self._settings(tuner.cache[key]):
+                    level = self._count_groups(*args)
+            else:
+                # First level of this shape: count it under every setting, keep the fastest.
+                best = None
+                for setting in tuner.settings(self.method):
+                    with self._settings(setting):
+                        torch.cuda.synchronize()
+                        t1 = time.perf_counter()
+                        trial = self._count_groups(*args)
+                        torch.cuda.synchronize()
+                        dt = time.perf_counter() - t1
+                    tuner.trials.append({"key": key, **setting, "s": dt})
+                    if best is None or dt < best[0]:
+                        best = (dt, setting, trial)
+                tuner.cache[key] = best[1]
+                level = best[2]
+        stats.ms = (time.perf_counter() - t0) * 1e3
+        stats.n_frequent = level.n
+        return level, stats
+
+    def _settings(self, setting: dict):
+        """Context manager applying tuned attributes (small_group, proj_density) for one count."""
+        engine = self
+
+        class _Apply:
+            def __enter__(self):
+                self.saved = {k: getattr(engine, k) for k in setting}
+                for k, v in setting.items():
+                    setattr(engine, k, v)
+
+            def __exit__(self, *exc):
+                for k, v in self.saved.items():
+                    setattr(engine, k, v)
+
+        return _Apply()
+
+    def _count_groups(self, gen, fbv, ldp, n_words, mc, infer, prune, n_rows, G, total, grp_first, grp_size,
+                      cand_off, sizes, offs, stats) -> Level:
+        """The counting of a level's candidates given its groups (see ``count_level``)."""
+        width = gen.k
+        stats.n_chunks = 0
+        out_rows = torch.empty((0, width + 1), dtype=torch.int32, device=self.device)
+        out_counts = torch.empty(0, dtype=torch.int32, device=self.device)
         # The subset test has prefix subsets to look up only from K=3 on.
         classify = (infer or prune) and width >= 2
         mode = (1 if prune or infer else 0) | (2 if infer else 0)
@@ -487,7 +548,16 @@ class Engine:
             ids = np.arange(g0, g1, dtype=np.int64)
             small = m <= self.small_group
             pr = proj[g0:g1]
-            for kind, sel in (("cands", small), ("tiles", ~small & ~pr), ("proj", pr & ~small)):
+            k2_rows = width == 1 and self._k2_rows is not None
+            if k2_rows:
+                # K=2 from the transactions (one group of every generator): pair counts by row-wise increments.
+                rp, cl, nnz, lut, n_r = self._k2_rows
+                n_g = int(sizes[0])
+                st = self._launch("pair_counts_rows", nnz * 8 + n_r * 8 + n_c * 4, lambda: self.lib.etm_pair_counts_rows(
+                    _p(rp), _p(cl), nnz, _p(lut), lut.numel(), n_r, n_g, _p(counts), _stream()))
+                check(st, "etm_pair_counts_rows")
+                self.launches += 1
+            for kind, sel in (() if k2_rows else (("cands", small), ("tiles", ~small & ~pr), ("proj", pr & ~small))):
                 gids = ids[sel]
                 if len(gids) == 0:
                     continue
@@ -563,10 +633,7 @@ class Engine:
             st = self.lib.etm_device_status(_stream())
             if st != 0:
                 raise RuntimeError(f"tensor-core counting failed: {self.lib.etm_last_error().decode()}")
-        level = Level(out_rows[:n_out], out_counts[:n_out])
-        stats.n_frequent = n_out
-        stats.ms = (time.perf_counter() - t0) * 1e3
-        return level, stats
+        return Level(out_rows[:n_out], out_counts[:n_out])
 
     def finish_level(self, new: Level, gen: Level, track_free: bool, prune: bool) -> Level:
         """Free flags against the generating level; under the free-set prune keep the free rows
@@ -599,8 +666,12 @@ class Engine:
     # -- the whole mine ----------------------------------------------------------
     def mine(self, bitvecs, n_rows: int, min_support: float, max_length: int | None = None, *,
              prune_equal_support: bool = False, use_generator_pruning: bool = False,
-             level_callback=None, n_cols_logical: int | None = None) -> MineOutput:
+             level_callback=None, n_cols_logical: int | None = None, rows=None) -> MineOutput:
+        """Mine device bitvectors. ``rows`` = (row_ptr int64, cols int32, host row lengths) on the device,
+        the transactions the bitvectors were built from, lets K=2 count row-wise when its rows are short
+        against the pair space (the reference's rule, gpu/row_split_chunks.py:124-142)."""
         ptr, (n_cols, ld), _owner = as_device_bitvecs(bitvecs)
+        self._k2_rows = None
         if n_rows >= 2**31:
             raise ValueError(f"n_transactions={n_rows:,} exceeds int32 max: the count arrays are int32")
         n_words = (n_rows + 63) // 64
@@ -625,6 +696,15 @@ class Engine:
             return out
         fbv, ldp = self.gather(ptr, ld, gen_cols, n_words)
         ng = len(gen_cols)
+        if rows is not None and self.k2_rows_max_r > 0:
+            rp, cl, lens = rows
+            pair_work = float((lens.astype(np.float64) * (lens - 1) / 2).sum())
+            r = pair_work / max(1.0, ng * (ng - 1) / 2 * n_words)
+            if r < self.k2_rows_max_r:
+                lut = torch.full((max(1, n_cols),), -1, dtype=torch.int32, device=self.device)
+                lut[torch.from_numpy(gen_cols.astype(np.int64)).to(self.device)] = torch.arange(
+                    ng, dtype=torch.int32, device=self.device)
+                self._k2_rows = (rp, cl, int(cl.numel()), lut, int(rp.numel()) - 1)
         gen = Level(torch.arange(ng, dtype=torch.int32, device=self.device)[:, None].contiguous(),
                     torch.from_numpy(col_counts[gen_cols].astype(np.int32)).to(self.device),
                     torch.from_numpy(free1[free1] if prune else free1).to(self.device).to(torch.uint8))
@@ -649,5 +729,5 @@ class Engine:
 def mine(bitvecs, n_rows: int, min_support: float, max_length: int | None = None, **kw) -> MineOutput:
     """Mine device bitvectors [n_cols, ceil(N/64)] with a fresh ``Engine`` (see ``Engine.mine``)."""
     engine_kw = {k: kw.pop(k) for k in ("method", "form", "chunk_cands", "small_group", "device", "project",
-                                        "proj_density", "proj_bytes", "tc_elem", "pipeline") if k in kw}
+                                        "proj_density", "proj_bytes", "tc_elem", "pipeline", "autotune") if k in kw}
     return Engine(**engine_kw).mine(bitvecs, n_rows, min_support, max_length, **kw)

@@ -154,6 +154,18 @@ int etm_count_cands(const uint64_t* fbv, int64_t ld, int64_t n_words, const int3
                     const uint8_t* cls, int32_t* out_counts, void* stream);
 
 /*
+ * Row-wise K=2: every row adds 1 to each pair of its generator columns.
+ * Replaces count_pairs_k2_rows (gpu/kernels/_src/pairs_k2_rows.cu:54; dispatch
+ * gpu/row_split_chunks.py:124-142). row_ptr int64 [n_rows+1] / cols int32
+ * [nnz]: the transactions' columns, ascending per row; lut int32 [lut_size]
+ * maps a column to its generator index or -1 (NULL: columns are generator
+ * indices). out_counts int32 [C(n_gen,2)] is zeroed here, then holds every
+ * pair's count at its lexicographic slot (the K=2 candidate index).
+ */
+int etm_pair_counts_rows(const int64_t* row_ptr, const int32_t* cols, int64_t nnz, const int32_t* lut,
+                         int64_t lut_size, int64_t n_rows, int64_t n_gen, int32_t* out_counts, void* stream);
+
+/*
  * Prefix projection (the reference's projection counting of wide groups,
  * core/cpu_miner.py:720-791, on the device). For the listed groups (width >= 2):
  *   etm_prefix_counts  out_counts int64 [n_work] = rows holding the group's prefix

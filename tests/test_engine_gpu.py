@@ -20,6 +20,12 @@ pytestmark = pytest.mark.gpu
 CASES = [c["name"] for c in json.loads((Path(__file__).parent / "golden" / "cases.json").read_text())["cases"]]
 
 
+def _rows_engine(e):
+    """An engine that counts K=2 row-wise whenever the transactions are given."""
+    e.k2_rows_max_r = float("inf")
+    return e
+
+
 @pytest.fixture(scope="module")
 def engines(pkg):
     from importlib import import_module
@@ -31,6 +37,9 @@ def engines(pkg):
         "tiny": eng.Engine(form="batched", chunk_cands=97, small_group=3),
         "proj": eng.Engine(form="batched", small_group=2, proj_density=1.01, proj_bytes=1 << 14),
         "noproj": eng.Engine(form="batched", project=False),
+        "popcount": eng.Engine(method="popcount"),
+        "rows": _rows_engine(eng.Engine()),
+        "tuned": eng.Engine(autotune=import_module(pkg.__name__ + ".autotune").Autotuner(min_candidates=1)),
     }
 
 
@@ -49,7 +58,7 @@ def test_transactions_match_golden(pkg, golden_cases, engines, name):
         assert pairs == want
 
 
-@pytest.mark.parametrize("form", ["plain", "tiny", "proj", "noproj"])
+@pytest.mark.parametrize("form", ["plain", "tiny", "proj", "noproj", "popcount", "tuned", "rows"])
 @pytest.mark.parametrize("name", ["implication_plain", "implication_prune", "implication_infer", "plain_small_plain",
                                   "deep_sparse_small", "dense_k2_small", "word_tail_65"])
 def test_forms_match_golden(pkg, golden_cases, engines, name, form):
@@ -132,6 +141,23 @@ def test_validation_errors(pkg):
         pkg.apriori([[1]], bitvecs=(dev, {0: 1, 1: 2, 2: 3}, 100))
     with pytest.raises(ValueError, match="n_transactions"):
         pkg.apriori(bitvecs=(torch.zeros((1, 1), dtype=torch.uint64, device="cuda"), {0: 1}, 1 << 31))
+
+
+def test_autotuner_caches_its_choice(pkg, golden_cases, engines):
+    """A tuned engine counts each new level shape under every setting once, then reuses the winner."""
+    eng = engines["tuned"]
+    case = golden_cases["implication_plain"]
+    indptr, items, n_rows = case_input(pkg, case)
+    for _ in range(2):
+        got = pkg.apriori(table_of(indptr, items, n_rows), min_support=case["min_support"], use_gpu=True,
+                          engine=eng, warn_complexity=False)
+        assert digest_pairs(pkg.result_pairs(got, n_rows)) == case["digest"]
+    tuner = eng.autotuner
+    assert tuner.cache
+    per_key = {}
+    for t in tuner.trials:
+        per_key[t["key"]] = per_key.get(t["key"], 0) + 1
+    assert all(n == len(tuner.settings("tensor")) for n in per_key.values())
 
 
 def test_level_callback_and_profile(pkg):

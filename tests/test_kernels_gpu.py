@@ -240,3 +240,36 @@ def test_compaction_overflow_regrows(pkg):
     want = np.bitwise_count(bv.view(np.uint64)[ii] & bv.view(np.uint64)[jj]).sum(axis=1)
     assert new.n == len(ii) and stats.n_frequent == len(ii)
     assert np.array_equal(new.counts.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("max_len", [20, 700])
+def test_pair_counts_rows_match_host(pkg, lib, max_len):
+    """Row-wise K=2 (pairs_k2_rows.cu:54 restated): every pair count from the rows, through a column lut."""
+    import torch
+
+    rng = np.random.default_rng(max_len)
+    n_rows, n_cols = 3000, 900
+    lens = rng.integers(0, max_len, n_rows)
+    lens[::97] = max_len  # some rows beyond the 512-entry shared slice when max_len is 700
+    rows = [np.sort(rng.choice(n_cols, size=min(l, n_cols), replace=False)) for l in lens]
+    indptr = np.zeros(n_rows + 1, np.int64)
+    np.cumsum([len(r) for r in rows], out=indptr[1:])
+    cols = np.concatenate(rows).astype(np.int32)
+    keep = rng.random(n_cols) < 0.7  # columns that generate; the others map to -1
+    gen = np.flatnonzero(keep)
+    lut = np.full(n_cols, -1, np.int32)
+    lut[gen] = np.arange(len(gen), dtype=np.int32)
+    n_g = len(gen)
+    want = np.zeros((n_g, n_g), np.int64)
+    for r in rows:
+        g = lut[r]
+        g = g[g >= 0]
+        ii, jj = np.triu_indices(len(g), 1)
+        np.add.at(want, (g[ii], g[jj]), 1)
+    want = want[np.triu_indices(n_g, 1)]
+    out = torch.full((len(want),), -7, dtype=torch.int32, device="cuda")
+    d = [_dev(indptr), _dev(cols), _dev(lut)]
+    st = lib.etm_pair_counts_rows(d[0].data_ptr(), d[1].data_ptr(), len(cols), d[2].data_ptr(), n_cols, n_rows, n_g,
+                                  out.data_ptr(), _stream())
+    assert st == 0, lib.etm_last_error()
+    assert np.array_equal(out.cpu().numpy(), want)
