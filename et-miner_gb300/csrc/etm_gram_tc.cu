@@ -9,7 +9,7 @@
 //   warps 0-7  producers: per stage (K = 64 transactions for f16, 128 for
 //              e4m3) thread t expands row t % 128 of A (t < 128) or of B: its
 //              words (prefetched a batch of 4 stages ahead into registers) become
-//              0.0/1.0 elements in the 128-byte swizzled K-major shared-memory
+//              0 / s elements in the 128-byte swizzled K-major shared-memory
 //              layout the MMA reads (SWIZZLE_128B), then fence.proxy.async and
 //              an mbarrier arrive. Two producer warps per scheduler hide the
 //              latency of the expansion chains. (Variant A_TMEM: A rows go from
@@ -24,9 +24,10 @@
 //              half (warp / 4), f32 -> int32, the i < j pair counts written at
 //              their lexicographic slots.
 //
-// Exactness: every product is 0 or 1 and every partial sum is an integer
-// below 2^24 (the caller sends only groups of at most 2^24 rows here), so the
-// f32 accumulation is exact.
+// Exactness: a set bit is stored as the format's smallest subnormal s
+// (f16 2^-24, e4m3 2^-9), so every product is 0 or s^2 and every partial sum
+// is c * s^2 with an integer c below 2^24 (the caller sends only groups of at
+// most 2^24 rows here): exact in f32, and scaled back exactly to c.
 //
 // Every mbarrier wait is bounded: after WAIT_LIMIT polls the block raises an
 // abort flag, every thread leaves its loop, the MMA thread waits (bounded) for
@@ -156,17 +157,24 @@ __device__ __forceinline__ void mma(uint32_t tmem_d, uint32_t tmem_a, uint64_t b
     }
 }
 
-// One operand row as 32 32-bit words: bits of x0 (and x1 for e4m3) expanded to 1.0 / 0 elements.
+// A set bit becomes the format's smallest positive subnormal (f16 0x0001 = 2^-24, e4m3 0x01 = 2^-9): the
+// expansion is then the bare bit spread, with no multiply. Every product is one power of two (2^-48 or
+// 2^-18), a count c accumulates to exactly c * 2^-48 or c * 2^-18 in f32 (c < 2^24), and the epilogue
+// scales back exactly.
+template <int ELEM>
+__device__ __forceinline__ constexpr float count_scale() { return ELEM == 2 ? 281474976710656.0f : 262144.0f; }
+
+// One operand row as 32 32-bit words: bits of x0 (and x1 for e4m3) expanded to elements.
 template <int ELEM>
 __device__ __forceinline__ void expand_row(uint64_t x0, uint64_t x1, uint32_t* w) {
 #pragma unroll
     for (int c = 0; c < 32; c++) {
         if constexpr (ELEM == 2) {
             const uint32_t t = (uint32_t)(x0 >> (2 * c)) & 3u;
-            w[c] = ((t & 1u) * 0x3C00u) | ((t >> 1) * 0x3C000000u);
+            w[c] = (t & 1u) | ((t >> 1) << 16);  // f16 0x0001 = 2^-24 per set bit
         } else {
             const uint32_t nib = (uint32_t)((c < 16 ? x0 : x1) >> (4 * (c & 15))) & 0xFu;
-            w[c] = ((nib * 0x00204081u) & 0x01010101u) * 0x38u;
+            w[c] = (nib * 0x00204081u) & 0x01010101u;  // e4m3 0x01 = 2^-9 per set bit
         }
     }
 }
@@ -188,7 +196,7 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                  : "memory");
 }
 
-// 16 bytes of operand elements from bits [0, 16/ELEM) of v: 1.0 (f16 0x3C00 / e4m3 0x38) or 0.
+// 16 bytes of operand elements from bits [0, 16/ELEM) of v: the smallest subnormal (f16 0x0001, e4m3 0x01) or 0.
 template <int ELEM>
 __device__ __forceinline__ uint4 expand_chunk(uint32_t v) {
     uint4 o;
@@ -198,16 +206,16 @@ __device__ __forceinline__ uint4 expand_chunk(uint32_t v) {
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const uint32_t t = (v >> (2 * q)) & 3u;
-            w[q] = ((t & 1u) * 0x3C00u) | ((t >> 1) * 0x3C000000u);
+            w[q] = (t & 1u) | ((t >> 1) << 16);
         }
         o = make_uint4(w[0], w[1], w[2], w[3]);
     } else {
-        // 16 bits -> 16 bytes: four bits per 32-bit word, spread to one bit per byte, times 0x38.
+        // 16 bits -> 16 bytes: four bits per 32-bit word, spread to one bit per byte.
         uint32_t w[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const uint32_t nib = (v >> (4 * q)) & 0xFu;
-            w[q] = ((nib * 0x00204081u) & 0x01010101u) * 0x38u;
+            w[q] = (nib * 0x00204081u) & 0x01010101u;
         }
         o = make_uint4(w[0], w[1], w[2], w[3]);
     }
@@ -400,7 +408,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gram_tc_kernel(
                             if (i < j && j < m) {
                                 const int64_t t = cb + tri_index(i, j, m);
                                 if (cls == nullptr || cls[t] == ETM_CAND_COUNT)
-                                    out[t] = n_stages > 0 ? __float2int_rn(__uint_as_float(v[c])) : 0;
+                                    out[t] = n_stages > 0 ? __float2int_rn(__uint_as_float(v[c]) * count_scale<ELEM>()) : 0;
                             }
                         }
                     }
