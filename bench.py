@@ -278,6 +278,8 @@ def main() -> None:
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparator")
     ap.add_argument("--proj-gb", type=float, default=4.0, help="device GB of projected words per chunk")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-pipeline", action="store_true",
+                    help="project and count chunks in turn on one stream (per-kernel times without overlap)")
     args = ap.parse_args()
     if args.workload == "serving":
         if args.impl == "reference":
@@ -313,7 +315,8 @@ def main() -> None:
     method = args.method or engm.DEFAULT_METHOD
     bv = dense_k2_device(pkg, lib, spec)
     n_rows = spec["n_rows"]
-    eng = engm.Engine(form="batched", method=method, tc_elem=args.tc_elem, proj_bytes=int(args.proj_gb * (1 << 30)))
+    eng = engm.Engine(form="batched", method=method, tc_elem=args.tc_elem, proj_bytes=int(args.proj_gb * (1 << 30)),
+                      pipeline=not args.no_pipeline)
     eng.profile_kernels = True
 
     def one(e):

@@ -1,14 +1,19 @@
 // Prefix projection: count a prefix group over only the transactions its
 // prefix holds. The reference's CPU route does this for wide groups
 // (_count_group_proj, core/cpu_miner.py:720-791: a Gram over the prefix's
-// tidset); here it is three device passes per chunk of groups:
+// tidset); here it is device passes per chunk of groups:
 //
-//   1. prefix counts:  popcount of the AND of the group's prefix columns
-//                      (sizes the row lists; coalesced 16-byte reads)
-//   2. prefix rows:    the ascending transaction ids of that AND (block scan
-//                      of per-word popcounts, then each word's bit positions)
-//   3. projection:     for every member, the bits of its column at those rows,
-//                      packed 64 per word by two warp ballots per 64 rows
+//   1. prefix counts:    popcount of the AND of the group's prefix columns
+//                        (plans the chunks; coalesced reads)
+//   2. prefix segments:  the same popcount per segment of ETM_PROJ_SEG_WORDS
+//                        words, giving each segment's piece of the projected
+//                        row its word offset
+//   3. projection:       per (segment, group): the segment's prefix rows listed
+//                        in shared memory; per member its segment words staged
+//                        in shared memory with cp.async and gathered at the
+//                        listed rows, 64 per word by two warp ballots
+//   (prefix rows:        the ascending transaction ids of the prefix AND, kept
+//                        as an entry point for callers that want the tidset)
 //
 // after which the tile-pair kernel counts the group on words that hold only
 // the prefix's rows: a group whose prefix holds a fraction d of the rows
@@ -82,60 +87,289 @@ __global__ void __launch_bounds__(PT) prefix_rows_kernel(const uint64_t* __restr
     }
 }
 
-constexpr int MB = 8;  // members per warp: the row-list loads are shared and 2 * MB gathers are in flight
+// Segmented projection. The rows are cut into segments of SEG_W bitvector words (64 SEG_W rows); the
+// projected row of a member is the concatenation over the segments of its bits at the prefix rows of
+// that segment, each segment's piece zero-padded to whole 64-bit words (zero rows add nothing to a
+// count). Units are (segment, work entry) in segment-major order, so the CTAs running at one time read
+// the same row range of the columns and the column words stay in L2 between groups.
+constexpr int SEG_W = ETM_PROJ_SEG_WORDS;
+constexpr int LIST_CAP = 8192;         // prefix rows listed per pass (a segment holds at most 64 SEG_W)
+constexpr int MPI = 4;                 // members gathered per block barrier (independent chains)
+constexpr int NSTAGE = 2 * MPI;        // member segments in shared memory: the current MPI and the next MPI
+constexpr int STAGE_BYTES = SEG_W * 8 + 16;  // a member's segment words, then 16 zero bytes
+constexpr int ID_RING = 512;           // member column ids held in shared memory
+constexpr int MAX_CHUNKS = (LIST_CAP / 64 / 4 + (PT / 32) - 1) / (PT / 32);
+constexpr int P_WARPS = PT / 32;
+constexpr int PROJ_SMEM = STAGE_BYTES * NSTAGE + SEG_W * 8 + LIST_CAP * 2;
 
-// One warp per (work entry, block of MB members): the members' column bits at the prefix's rows.
-// mblk_off is the exclusive prefix of ceil(m / MB) over the work entries.
-__global__ void __launch_bounds__(PT) project_kernel(const uint64_t* __restrict__ fbv, int64_t ld,
-                                                     const int32_t* __restrict__ rows, int width,
-                                                     const int64_t* __restrict__ grp_first,
-                                                     const int32_t* __restrict__ grp_size,
-                                                     const int64_t* __restrict__ work_groups,
-                                                     const int64_t* __restrict__ mblk_off, int64_t n_work,
-                                                     const int64_t* __restrict__ row_off,
-                                                     const int32_t* __restrict__ rowidx,
-                                                     const int64_t* __restrict__ cbase, const int64_t* __restrict__ cld,
-                                                     uint64_t* __restrict__ cbuf) {
-    const int lane = threadIdx.x & 31;
-    const int64_t total = mblk_off[n_work];
-    const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < total; q += n_warps) {
-        const int64_t wi = upper_find(mblk_off, n_work, q);
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// One block per work entry: the words of every segment's piece, their exclusive prefix (seg_off, n_seg + 1
+// entries per work entry) and the total (out_words).
+__global__ void __launch_bounds__(PT) prefix_segments_kernel(const uint64_t* __restrict__ fbv, int64_t ld,
+                                                             int64_t n_words, const int32_t* __restrict__ rows,
+                                                             int width, const int64_t* __restrict__ grp_first,
+                                                             const int64_t* __restrict__ work_groups, int64_t n_seg,
+                                                             int64_t* __restrict__ seg_off,
+                                                             int64_t* __restrict__ out_words) {
+    __shared__ int32_t pref[64];
+    __shared__ unsigned part[P_WARPS];
+    const int64_t wi = blockIdx.x;
+    const int64_t first = grp_first[work_groups[wi]];
+    const int plen = width - 1;
+    if (threadIdx.x < plen) pref[threadIdx.x] = rows[first * width + threadIdx.x];
+    __syncthreads();
+    int64_t* so = seg_off + wi * (n_seg + 1);
+    int64_t run = 0;  // meaningful in thread 0
+    for (int64_t s = 0; s < n_seg; s++) {
+        const int64_t w1 = min64(n_words, (s + 1) * SEG_W);
+        unsigned c = 0;
+        for (int64_t w = s * SEG_W + threadIdx.x; w < w1; w += PT) c += __popcll(prefix_word(fbv, ld, pref, plen, w));
+        c = __reduce_add_sync(0xffffffffu, c);
+        if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned t = 0;
+            for (int i = 0; i < P_WARPS; i++) t += part[i];
+            so[s] = run;
+            run += (t + 63) / 64;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        so[n_seg] = run;
+        out_words[wi] = run;
+    }
+}
+
+struct PassArgs {
+    const uint64_t* fbv;
+    int64_t ld;
+    const int32_t* rows;
+    int width;
+    int64_t first, m, w0;
+    int nw;
+    uint64_t* stage;
+    const uint32_t* l32;
+    int pass_rows, pass_words;
+    uint64_t* dst;
+    int64_t stride, out0;
+    uint64_t* park;  // MPI x 4 MAX_CHUNKS words per warp of shared memory
+    int32_t* ids;    // ID_RING member column ids (shared memory)
+};
+
+// Every member of the group through the stage buffers, for one pass of listed rows. The pass's output
+// words go to the warps in chunks of 4 (chunk c to warp c % P_WARPS, at most MAX_CHUNKS per warp).
+// Per lane and word, the stage-buffer byte offset of the 32-bit word holding each of its two rows and
+// the row's bit are computed once per pass; rows past the pass point at the zero pad after the
+// buffer. Per member a word then costs two shared loads, two bit tests and two ballots; members go MPI
+// at a time (independent chains, one block barrier per MPI members); lane 0 parks the words in shared
+// memory and the warp stores them with coalesced stores.
+__device__ __forceinline__ void gather_members(const PassArgs& a) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int m = (int)a.m;
+    const int n_chunks = (a.pass_words + 3) >> 2;
+    uint32_t ra[MAX_CHUNKS * 4], rb[MAX_CHUNKS * 4], ma[MAX_CHUNKS * 4], mb[MAX_CHUNKS * 4];
+    uint32_t valid = 0;  // bit 4 k + q: word q of the warp's k-th chunk is a word of the pass
+#pragma unroll
+    for (int k = 0; k < MAX_CHUNKS; k++) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int i = 4 * k + q;
+            const int t = 4 * (warp + P_WARPS * k) + q;
+            const int r0 = 64 * t + lane, r1 = r0 + 32;
+            const uint32_t e = t < a.pass_words ? a.l32[32 * t + lane] : 0u;
+            const uint32_t l0 = e & 0xFFFFu, l1 = e >> 16;
+            ra[i] = r0 < a.pass_rows ? (l0 >> 5) << 2 : SEG_W * 8;  // else the zero pad
+            rb[i] = r1 < a.pass_rows ? (l1 >> 5) << 2 : SEG_W * 8;
+            ma[i] = 1u << (l0 & 31u);
+            mb[i] = 1u << (l1 & 31u);
+            valid |= (t < a.pass_words ? 1u : 0u) << i;
+        }
+    }
+    // Copies: member j's segment words into stage buffer j % NSTAGE, 16 bytes per thread and step, MPI
+    // members per commit group. One group per MPI members (empty past the last member), so the wait
+    // below always leaves NSTAGE / MPI - 2 groups pending and the current members' copies have landed. Member
+    // column ids come from a ring of ID_RING entries in shared memory, refilled half a ring ahead (its
+    // global latency is paid once per ID_RING / 2 members, not per member).
+    const int32_t* colp = a.rows + a.first * a.width + a.width - 1;
+    const int n16 = a.nw >> 1;
+    const bool odd = (a.nw & 1) && threadIdx.x == 0;
+    auto copy = [&](int j, int buf) {
+        if (j < m) {
+            const uint64_t* src = a.fbv + (int64_t)a.ids[j & (ID_RING - 1)] * a.ld + a.w0;
+            uint8_t* d = reinterpret_cast<uint8_t*>(a.stage) + buf * STAGE_BYTES;
+            for (int i = threadIdx.x; i < n16; i += PT) cp_async16(d + 16 * i, src + 2 * i);
+            if (odd) cp_async8(d + 8 * (a.nw - 1), src + a.nw - 1);
+        }
+    };
+    auto fill_ids = [&](int j1) {  // members [j1, j1 + ID_RING / 2)
+        for (int t = threadIdx.x; t < ID_RING / 2; t += PT) {
+            const int j = j1 + t;
+            a.ids[j & (ID_RING - 1)] = j < m ? colp[(int64_t)j * a.width] : 0;
+        }
+    };
+    fill_ids(0);
+    fill_ids(ID_RING / 2);
+    __syncthreads();
+#pragma unroll
+    for (int d = 0; d < NSTAGE - MPI; d += MPI) {
+#pragma unroll
+        for (int v = 0; v < MPI; v++) copy(d + v, d + v);
+        cp_async_commit();
+    }
+    const uint8_t* sbytes = reinterpret_cast<const uint8_t*>(a.stage);
+    uint64_t* park = a.park + warp * MPI * 4 * MAX_CHUNKS;
+    const bool my_store = lane < 4 * MAX_CHUNKS && ((valid >> lane) & 1u);
+    uint64_t* out = a.dst + a.out0 + 4 * (warp + P_WARPS * (lane >> 2)) + (lane & 3);
+    for (int j0 = 0; j0 < m; j0 += NSTAGE) {
+        // Unrolled over the stage buffers: members j0 + u .. j0 + u + MPI - 1 sit in buffers u ...
+#pragma unroll
+        for (int u = 0; u < NSTAGE; u += MPI) {
+            const int j = j0 + u;
+            if (j >= m) break;
+            cp_async_wait<NSTAGE / MPI - 2>();
+            __syncthreads();  // members j .. j + MPI - 1 visible to all; every warp is past the previous ones
+#pragma unroll
+            for (int v = 0; v < MPI; v++)  // into the buffers of the previous MPI members
+                copy(j + NSTAGE - MPI + v, (u + NSTAGE - MPI + v) % NSTAGE);
+            cp_async_commit();
+            if ((j & (ID_RING / 2 - 1)) == 0 && j > 0) fill_ids(j + ID_RING / 2);
+            const uint8_t* sa = sbytes + u * STAGE_BYTES;
+#pragma unroll
+            for (int k = 0; k < MAX_CHUNKS; k++) {
+                if (warp + P_WARPS * k >= n_chunks) break;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int i = 4 * k + q;
+                    uint32_t x0[MPI], x1[MPI];
+#pragma unroll
+                    for (int v = 0; v < MPI; v++) {
+                        x0[v] = *reinterpret_cast<const uint32_t*>(sa + v * STAGE_BYTES + ra[i]);
+                        x1[v] = *reinterpret_cast<const uint32_t*>(sa + v * STAGE_BYTES + rb[i]);
+                    }
+#pragma unroll
+                    for (int v = 0; v < MPI; v++) {
+                        const unsigned lo = __ballot_sync(0xffffffffu, (x0[v] & ma[i]) != 0u);
+                        const unsigned hi = __ballot_sync(0xffffffffu, (x1[v] & mb[i]) != 0u);
+                        if (lane == 0) park[v * 4 * MAX_CHUNKS + i] = (uint64_t)lo | ((uint64_t)hi << 32);
+                    }
+                }
+            }
+            __syncwarp();
+            if (my_store) {
+#pragma unroll
+                for (int v = 0; v < MPI; v++)
+                    if (j + v < m) out[v * a.stride] = park[v * 4 * MAX_CHUNKS + lane];
+            }
+            out += MPI * a.stride;
+            __syncwarp();
+        }
+    }
+    cp_async_wait<0>();
+}
+
+// Unit (segment s, work entry wi): the prefix words of the segment, the list of its prefix rows (local
+// row ids, 16 bits), both in shared memory, then for every member its segment words staged in
+// shared memory (cp.async, NSTAGE buffers, NSTAGE - 1 members ahead) and gathered at the listed rows
+// with two ballots per 64 rows. Warp w writes a contiguous run of output words, one per lane.
+__global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __restrict__ fbv, int64_t ld,
+                                                         int64_t n_words, const int32_t* __restrict__ rows,
+                                                         int width, const int64_t* __restrict__ grp_first,
+                                                         const int32_t* __restrict__ grp_size,
+                                                         const int64_t* __restrict__ work_groups, int64_t n_work,
+                                                         int64_t n_seg, const int64_t* __restrict__ seg_off,
+                                                         const int64_t* __restrict__ cbase,
+                                                         const int64_t* __restrict__ cld,
+                                                         uint64_t* __restrict__ cbuf) {
+    extern __shared__ __align__(16) uint8_t psmem[];
+    uint64_t* stage = reinterpret_cast<uint64_t*>(psmem);  // NSTAGE x (SEG_W member words + zero pad)
+    uint64_t* pw = reinterpret_cast<uint64_t*>(psmem + NSTAGE * STAGE_BYTES);  // SEG_W prefix words
+    uint16_t* list = reinterpret_cast<uint16_t*>(pw + SEG_W);
+    __shared__ int32_t pref[64];
+    __shared__ uint64_t park[P_WARPS * MPI * 4 * MAX_CHUNKS];
+    __shared__ int32_t ids[ID_RING];
+    const int plen = width - 1;
+    const int64_t total = n_seg * n_work;
+    if (threadIdx.x < 2 * NSTAGE)  // the zero pads after the stage buffers (cp.async never writes them)
+        reinterpret_cast<uint64_t*>(psmem + (threadIdx.x >> 1) * STAGE_BYTES + SEG_W * 8)[threadIdx.x & 1] = 0ULL;
+    for (int64_t q = blockIdx.x; q < total; q += gridDim.x) {
+        const int64_t s = q / n_work, wi = q - s * n_work;
         const int64_t g = work_groups[wi];
         const int64_t m = grp_size[g];
-        const int64_t i0 = (q - mblk_off[wi]) * MB;
-        const int nm = (int)min64(MB, m - i0);
-        const int32_t* R = rowidx + row_off[wi];
-        const int64_t n = row_off[wi + 1] - row_off[wi];
-        const int64_t stride = cld[wi];
         const int64_t first = grp_first[g];
-        const uint64_t* src[MB];
+        const int64_t w0 = s * SEG_W;
+        const int nw = (int)min64(SEG_W, n_words - w0);
+        const int64_t* so = seg_off + wi * (n_seg + 1);
+        const int64_t stride = cld[wi];
+        uint64_t* dst = cbuf + cbase[wi] + so[s];
+        __syncthreads();  // the previous unit is done with the shared buffers
+        if (threadIdx.x < plen) pref[threadIdx.x] = rows[first * width + threadIdx.x];
+        __syncthreads();
+        int my = 0;
 #pragma unroll
-        for (int j = 0; j < MB; j++) {
-            const int64_t col = rows[(first + i0 + (j < nm ? j : 0)) * width + width - 1];
-            src[j] = fbv + col * ld;
+        for (int k = 0; k < SEG_W / PT; k++) {
+            const int w = threadIdx.x * (SEG_W / PT) + k;
+            const uint64_t p = w < nw ? prefix_word(fbv, ld, pref, plen, w0 + w) : 0ULL;
+            pw[w] = p;
+            my += __popcll(p);
         }
-        uint64_t* dst = cbuf + cbase[wi] + i0 * stride;
-        const int64_t nw = (n + 63) >> 6;
-        for (int64_t t = 0; t < nw; t++) {
-            const int64_t e0 = t * 64 + lane, e1 = e0 + 32;
-            const int32_t r0 = e0 < n ? __ldg(R + e0) : -1;
-            const int32_t r1 = e1 < n ? __ldg(R + e1) : -1;
-            uint64_t x0[MB], x1[MB];
+        int64_t cnt;
+        const int64_t my_base = block_exclusive_scan(my, &cnt);
+        for (int64_t p0 = 0; p0 < cnt; p0 += LIST_CAP) {
+            // The prefix rows [p0, p0 + LIST_CAP) of the segment, as local row ids.
+            int64_t at = my_base;
 #pragma unroll
-            for (int j = 0; j < MB; j++) {
-                x0[j] = r0 >= 0 ? __ldg(src[j] + (r0 >> 6)) : 0ULL;
-                x1[j] = r1 >= 0 ? __ldg(src[j] + (r1 >> 6)) : 0ULL;
+            for (int k = 0; k < SEG_W / PT; k++) {
+                const int w = threadIdx.x * (SEG_W / PT) + k;
+                uint64_t bits = pw[w];
+                const int c = __popcll(bits);
+                if (at + c > p0 && at < p0 + LIST_CAP) {
+                    int64_t a = at;
+                    while (bits) {
+                        const int b = __ffsll((long long)bits) - 1;
+                        if (a >= p0 && a < p0 + LIST_CAP) {
+                            // Interleaved: rows 64 t + l and 64 t + 32 + l share 32-bit entry 32 t + l.
+                            const int64_t x = a - p0;
+                            list[((x >> 6) << 6) + ((x & 31) << 1) + ((x >> 5) & 1)] = (uint16_t)(w * 64 + b);
+                        }
+                        ++a;
+                        bits &= bits - 1;
+                    }
+                }
+                at += c;
             }
-#pragma unroll
-            for (int j = 0; j < MB; j++) {
-                const unsigned lo = __ballot_sync(0xffffffffu, (unsigned)(x0[j] >> (r0 & 63)) & 1u);
-                const unsigned hi = __ballot_sync(0xffffffffu, (unsigned)(x1[j] >> (r1 & 63)) & 1u);
-                if (lane == j && j < nm) dst[j * stride + t] = (uint64_t)lo | ((uint64_t)hi << 32);
+            const int pass_rows = (int)min64(LIST_CAP, cnt - p0);
+            const int pass_words = (pass_rows + 63) >> 6;
+            // Entries past the pass's last row name local row 0 (an in-range word); the store masks their bits.
+            for (int x = pass_rows + threadIdx.x; x < ((pass_words + 3) & ~3) * 64; x += PT)
+                list[((x >> 6) << 6) + ((x & 31) << 1) + ((x >> 5) & 1)] = 0;
+            __syncthreads();
+            const PassArgs pa{fbv, ld, rows, width, first, m, w0, nw, stage, reinterpret_cast<const uint32_t*>(list),
+                              pass_rows, pass_words, dst, stride, p0 >> 6, park, ids};
+            gather_members(pa);
+            cp_async_wait<0>();
+            __syncthreads();  // the next pass rewrites the list
+        }
+        if (s == n_seg - 1) {
+            // Zero the words after the last piece, up to the member stride.
+            const int64_t used = so[n_seg];
+            const int64_t pad = stride - used;
+            uint64_t* row0 = cbuf + cbase[wi] + used;
+            for (int64_t idx = threadIdx.x; idx < m * pad; idx += PT) {
+                const int64_t j = idx / pad;
+                row0[j * stride + (idx - j * pad)] = 0ULL;
             }
         }
-        for (int j = 0; j < nm; j++)
-            for (int64_t w = nw + lane; w < stride; w += 32) dst[j * stride + w] = 0ULL;
     }
 }
 
@@ -167,15 +401,39 @@ extern "C" int etm_prefix_rows(const uint64_t* fbv, int64_t ld, int64_t n_words,
     return ETM_OK;
 }
 
-extern "C" int etm_project(const uint64_t* fbv, int64_t ld, const int32_t* rows, int32_t width,
-                           const int64_t* grp_first, const int32_t* grp_size, const int64_t* work_groups,
-                           const int64_t* mblk_off, int64_t n_work, const int64_t* row_off, const int32_t* row_idx,
-                           const int64_t* cbase, const int64_t* cld, uint64_t* cbuf, void* stream) {
-    ETM_REQUIRE(width >= 2 && width <= 64, ETM_EINVAL, "etm_project: width %d out of range (2..64)", width);
+extern "C" int etm_prefix_segments(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows,
+                                   int32_t width, const int64_t* grp_first, const int64_t* work_groups,
+                                   int64_t n_work, int64_t* seg_off, int64_t* out_words, void* stream) {
+    ETM_REQUIRE(width >= 2 && width <= 64, ETM_EINVAL, "etm_prefix_segments: width %d out of range (2..64)", width);
+    ETM_REQUIRE(ld >= n_words && n_words >= 0, ETM_EINVAL, "etm_prefix_segments: bad n_words / ld");
+    ETM_REQUIRE(n_work < (1LL << 31), ETM_EINVAL, "etm_prefix_segments: too many groups");
     if (n_work <= 0) return ETM_OK;
-    const int grid = max(1, sm_count()) * 8;
-    project_kernel<<<grid, PT, 0, as_stream(stream)>>>(fbv, ld, rows, width, grp_first, grp_size, work_groups,
-                                                       mblk_off, n_work, row_off, row_idx, cbase, cld, cbuf);
+    const int64_t n_seg = ceil_div<int64_t>(n_words, SEG_W);
+    prefix_segments_kernel<<<(unsigned)n_work, PT, 0, as_stream(stream)>>>(fbv, ld, n_words, rows, width, grp_first,
+                                                                           work_groups, n_seg, seg_off, out_words);
+    ETM_LAUNCHED("prefix_segments");
+    return ETM_OK;
+}
+
+extern "C" int etm_project(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                           const int64_t* grp_first, const int32_t* grp_size, const int64_t* work_groups,
+                           int64_t n_work, const int64_t* seg_off, const int64_t* cbase, const int64_t* cld,
+                           uint64_t* cbuf, void* stream) {
+    ETM_REQUIRE(width >= 2 && width <= 64, ETM_EINVAL, "etm_project: width %d out of range (2..64)", width);
+    ETM_REQUIRE(ld >= n_words && n_words >= 0 && ld % 2 == 0, ETM_EINVAL, "etm_project: ld must be even and >= n_words");
+    ETM_REQUIRE((reinterpret_cast<uintptr_t>(fbv) & 15) == 0, ETM_EINVAL, "etm_project: fbv must be 16-byte aligned");
+    if (n_work <= 0 || n_words == 0) return ETM_OK;
+    static bool configured = false;
+    if (!configured) {
+        ETM_CUDA(cudaFuncSetAttribute(project_seg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, PROJ_SMEM));
+        configured = true;
+    }
+    const int64_t n_seg = ceil_div<int64_t>(n_words, SEG_W);
+    const int64_t units = n_seg * n_work;
+    const int grid = (int)min64(units, (int64_t)max(1, sm_count()) * 2);
+    project_seg_kernel<<<grid, PT, PROJ_SMEM, as_stream(stream)>>>(fbv, ld, n_words, rows, width, grp_first, grp_size,
+                                                                   work_groups, n_work, n_seg, seg_off, cbase, cld,
+                                                                   cbuf);
     ETM_LAUNCHED("project");
     return ETM_OK;
 }

@@ -53,6 +53,7 @@ PROJ_BYTES = 4 << 30
 TC_TILE = 256
 #: Largest group (rows) the tensor-core Gram counts exactly: f32 holds every integer up to 2^24.
 TC_MAX_ROWS = 1 << 24
+PROJ_SEG_WORDS = 1024  # ETM_PROJ_SEG_WORDS: bitvector words per projection segment
 #: Row-wise K=2 crossover: rows' pair increments over pairs x words (the reference's K2_ROWS_MAX_R).
 K2_ROWS_MAX_R = 3.95e-3
 #: Counting method for tile-pairs: "popcount" or "tensor".
@@ -68,6 +69,13 @@ def mining_min_count(min_support: float, n_rows: int) -> int:
     """The threshold the levels apply: ``min_count``, at least 1, as the CPU route does
     (core/cpu_miner.py:967-970); at 0 every pair would be "frequent" with count 0."""
     return max(1, min_count(min_support, n_rows))
+
+
+def proj_stride(pcnt: np.ndarray, n_words: int) -> np.ndarray:
+    """Words per member of a projected group: its prefix rows in whole words, one padded word per
+    segment of PROJ_SEG_WORDS bitvector words, rounded up to 32 (at least 32)."""
+    n_seg = max(1, -(-int(n_words) // PROJ_SEG_WORDS))
+    return np.maximum(32, ((np.asarray(pcnt, np.int64) + 63) // 64 + n_seg + 31) // 32 * 32)
 
 
 def _tile_items(m: np.ndarray, method: int) -> np.ndarray:
@@ -321,7 +329,7 @@ class Engine:
         return out.cpu().numpy().copy()
 
     def _prep_projected(self, fbv, ldp, n_words, gen, grp_first, grp_size, gids, sizes, pcnt, method, buf: int = 0):
-        """Row lists and projected member words of the listed groups (two launches on the current stream).
+        """Segment offsets and projected member words of the listed groups (two launches on the current stream).
 
         Returns what ``_count_prepped`` needs. ``buf`` selects one of two scratch sets, so the
         projection of the next chunk can run while the current one is counted.
@@ -329,36 +337,36 @@ class Engine:
         width = gen.k
         m = sizes[gids]
         cnt = pcnt[gids]
-        cw = (cnt + 63) // 64
-        cl = np.maximum(32, (cw + 31) // 32 * 32)
-        row_off = np.zeros(len(gids) + 1, np.int64)
-        np.cumsum(cnt, out=row_off[1:])
-        mem_off = np.zeros(len(gids) + 1, np.int64)
-        np.cumsum((m + 7) // 8, out=mem_off[1:])
+        n_seg = max(1, -(-n_words // PROJ_SEG_WORDS))
+        cl = proj_stride(cnt, n_words)
         cb = np.zeros(len(gids) + 1, np.int64)
         np.cumsum(m * cl, out=cb[1:])
         toff = np.zeros(len(gids) + 1, np.int64)
         np.cumsum(_tile_items(m, method), out=toff[1:])
         n = len(gids)
-        host = np.concatenate([gids.astype(np.int64), toff, row_off, mem_off, cb[:-1], cw, cl])
+        # cwords starts as the bound (whole words of the prefix rows plus one padded word per segment);
+        # etm_prefix_segments overwrites it with the exact padded length.
+        host = np.concatenate([gids.astype(np.int64), toff, cb[:-1], (cnt + 63) // 64 + n_seg, cl])
         d = torch.from_numpy(host).to(self.device)
         wg, wo = d[:n], d[n:2 * n + 1]
-        ro, mo = d[2 * n + 1:3 * n + 2], d[3 * n + 2:4 * n + 3]
-        cbase, cwords, cld = d[4 * n + 3:5 * n + 3], d[5 * n + 3:6 * n + 3], d[6 * n + 3:7 * n + 3]
-        rowidx = self.scratch.get(f"proj_rows_{buf}", int(row_off[-1]), torch.int32)
+        cbase, cwords, cld = d[2 * n + 1:3 * n + 1], d[3 * n + 1:4 * n + 1], d[4 * n + 1:5 * n + 1]
+        seg_off = self.scratch.get(f"proj_seg_{buf}", n * (n_seg + 1), torch.int64)
         cbuf = self.scratch.get(f"proj_cbuf_{buf}", int(cb[-1]), torch.int64)
-        st = self._launch("prefix_rows", int(n * (width - 1) * n_words * 8 + row_off[-1] * 4),
-                          lambda: self.lib.etm_prefix_rows(_p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first),
-                                                           _p(wg), n, _p(ro), _p(rowidx), _stream()))
-        check(st, "etm_prefix_rows")
-        st = self._launch("project", int((m * cnt).sum() * 4 // 32 + (m * cl).sum() * 8 + (m * cnt).sum() // 8),
-                          lambda: self.lib.etm_project(_p(fbv), ldp, _p(gen.rows), width, _p(grp_first),
-                                                       _p(grp_size), _p(wg), _p(mo), n, _p(ro), _p(rowidx),
-                                                       _p(cbase), _p(cld), _p(cbuf), _stream()))
+        st = self._launch("prefix_segments", int(n * (width - 1) * n_words * 8),
+                          lambda: self.lib.etm_prefix_segments(_p(fbv), ldp, n_words, _p(gen.rows), width,
+                                                               _p(grp_first), _p(wg), n, _p(seg_off), _p(cwords),
+                                                               _stream()))
+        check(st, "etm_prefix_segments")
+        # Algorithmic bytes: every member's column words and the prefix words read once, the strides written.
+        st = self._launch("project", int(((m + width - 1) * n_words).sum() * 8 + (m * cl).sum() * 8),
+                          lambda: self.lib.etm_project(_p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first),
+                                                       _p(grp_size), _p(wg), n, _p(seg_off), _p(cbase), _p(cld),
+                                                       _p(cbuf), _stream()))
         check(st, "etm_project")
         self.launches += 2
         return dict(d=d, cbuf=cbuf, cbase=cbase, cwords=cwords, cld=cld, wg=wg, wo=wo, n=n, n_tiles=int(toff[-1]),
-                    nbytes=int((m * cw).sum() * 8), macs=float((m * (m - 1) / 2 * cnt.astype(np.float64)).sum()))
+                    nbytes=int((m * ((cnt + 63) // 64)).sum() * 8),
+                    macs=float((m * (m - 1) / 2 * cnt.astype(np.float64)).sum()))
 
     def _count_prepped(self, prep, grp_size, cand_off, base, cls, counts, method):
         """The tile-pair counts of a prepared projection (one launch on the current stream)."""
@@ -482,8 +490,8 @@ class Engine:
                 proj = big & (pcnt <= TC_MAX_ROWS)
             else:
                 proj = big & (pcnt < self.proj_density * n_rows)
-        pwords = np.maximum(32, ((pcnt + 63) // 64 + 31) // 32 * 32)
-        pbytes = np.where(proj, sizes * pwords * 8 + pcnt * 4, 0)
+        pwords = proj_stride(pcnt, n_words)
+        pbytes = np.where(proj, sizes * pwords * 8, 0)
         pcum = np.zeros(G + 1, np.int64)
         np.cumsum(pbytes, out=pcum[1:])
         cap = int(min(total, max(1 << 16, 2 * gen.n)))

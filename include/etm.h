@@ -55,6 +55,9 @@ extern "C" {
  * instead of shared memory. Exact either way; the shared-memory form is faster on GB300. */
 #define ETM_TC_A_TMEM 4
 
+/* Rows of one projection segment: 1024 bitvector words (65,536 transactions). */
+#define ETM_PROJ_SEG_WORDS 1024
+
 int etm_version(void);
 /* Message of the last failing call on this thread (empty if none). */
 const char* etm_last_error(void);
@@ -173,11 +176,18 @@ int etm_pair_counts_rows(const int64_t* row_ptr, const int32_t* cols, int64_t nn
  *   etm_prefix_rows    out_rows int32 = those rows, ascending, group wi at
  *                      [row_off[wi], row_off[wi+1]) (row_off: exclusive prefix of
  *                      the counts);
+ *   etm_prefix_segments  the prefix AND's popcount per segment of
+ *                      ETM_PROJ_SEG_WORDS words: seg_off int64 [n_work][n_seg+1]
+ *                      (n_seg = ceil(n_words / ETM_PROJ_SEG_WORDS)) = the word
+ *                      offset of each segment's piece of a projected row, each
+ *                      piece ceil(count / 64) words; out_words[wi] = the total;
  *   etm_project        member i of group wi -> cbuf[cbase[wi] + i*cld[wi] ...]:
- *                      its column's bits at the prefix rows, 64 per word, zero
- *                      padded to cld[wi] words (cld % 32 == 0, cbase even);
- *                      mblk_off int64 [n_work+1] = exclusive prefix of
- *                      ceil(m/8) (one warp gathers 8 members).
+ *                      per segment, its column's bits at the segment's prefix
+ *                      rows, 64 per word, the piece zero-padded to whole words
+ *                      at seg_off; zero from out_words[wi] up to cld[wi] words
+ *                      (cld % 32 == 0, cbase even, ld even, fbv 16-byte aligned).
+ *                      Padding rows are zero in every member, so pair counts
+ *                      over the projected words equal those over the prefix rows.
  *   etm_count_tiles_proj  etm_count_tiles over the projected words
  *                      (cwords[wi] words per member; no prefix AND).
  */
@@ -187,10 +197,12 @@ int etm_prefix_counts(const uint64_t* fbv, int64_t ld, int64_t n_words, const in
 int etm_prefix_rows(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
                     const int64_t* grp_first, const int64_t* work_groups, int64_t n_work, const int64_t* row_off,
                     int32_t* out_rows, void* stream);
-int etm_project(const uint64_t* fbv, int64_t ld, const int32_t* rows, int32_t width, const int64_t* grp_first,
-                const int32_t* grp_size, const int64_t* work_groups, const int64_t* mblk_off, int64_t n_work,
-                const int64_t* row_off, const int32_t* row_idx, const int64_t* cbase, const int64_t* cld,
-                uint64_t* cbuf, void* stream);
+int etm_prefix_segments(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                        const int64_t* grp_first, const int64_t* work_groups, int64_t n_work, int64_t* seg_off,
+                        int64_t* out_words, void* stream);
+int etm_project(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                const int64_t* grp_first, const int32_t* grp_size, const int64_t* work_groups, int64_t n_work,
+                const int64_t* seg_off, const int64_t* cbase, const int64_t* cld, uint64_t* cbuf, void* stream);
 int etm_count_tiles_proj(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                          const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
                          const int64_t* work_off, int64_t n_work, int64_t chunk_base, const uint8_t* cls,

@@ -273,3 +273,99 @@ def test_pair_counts_rows_match_host(pkg, lib, max_len):
                                   out.data_ptr(), _stream())
     assert st == 0, lib.etm_last_error()
     assert np.array_equal(out.cpu().numpy(), want)
+
+
+def _projection_reference(bits, ld, n_words, groups, stride):
+    """Per group (prefix columns, member columns): each member's bits at the prefix rows, per segment of
+    ETM_PROJ_SEG_WORDS words, every segment's piece padded to whole 64-bit words, zeros to the stride."""
+    seg = 1024
+    out = []
+    for (prefix, members), cl in zip(groups, stride):
+        mask = np.ones(n_words * 64, bool)
+        for c in prefix:
+            mask &= bits[c]
+        rows = []
+        for m in members:
+            words = []
+            for s0 in range(0, n_words * 64, seg * 64):
+                sel = bits[m][s0:s0 + seg * 64][mask[s0:s0 + seg * 64]]
+                if len(sel):
+                    pad = np.zeros((len(sel) + 63) // 64 * 64, np.uint8)
+                    pad[:len(sel)] = sel
+                    words.append(np.packbits(pad, bitorder="little").view(np.uint64))
+            w = np.concatenate(words) if words else np.zeros(0, np.uint64)
+            row = np.zeros(cl, np.uint64)
+            row[:len(w)] = w
+            rows.append(row)
+        out.append(np.stack(rows))
+    return out
+
+
+@pytest.mark.parametrize("n_words,width", [(1, 2), (1023, 2), (1024, 3), (1025, 2), (3001, 3), (2500, 2)])
+def test_segmented_projection(pkg, lib, n_words, width):
+    """etm_prefix_segments + etm_project against the host restatement, including a dense prefix (more
+    prefix rows in a segment than one pass lists), an empty prefix and the zero padding."""
+    import importlib
+
+    import torch
+
+    eng = importlib.import_module(pkg.__name__ + ".engine")
+    rng = np.random.default_rng(n_words * 10 + width)
+    n_cols = 14
+    dens = np.array([0.9, 0.5, 0.06, 0.02, 0.0, 0.3] + [0.4] * (n_cols - 6))
+    ld = max(32, (n_words + 31) // 32 * 32)
+    bits = (rng.random((n_cols, n_words * 64)) < dens[:, None]).astype(np.uint8)
+    words = np.packbits(bits, axis=1, bitorder="little").view(np.uint64)
+    fbv_h = rng.integers(0, 2**63, (n_cols, ld), dtype=np.int64).view(np.uint64)  # garbage past n_words
+    fbv_h[:, :n_words] = words
+    plen = width - 1
+    prefixes = [tuple(range(p, p + plen)) for p in (0, 1, 2, 3, 4)]
+    groups = []
+    level_rows = []
+    for pre in prefixes:
+        members = sorted(rng.choice(np.arange(plen + 4, n_cols), size=int(rng.integers(1, 7)), replace=False))
+        groups.append((pre, members))
+        for mbr in members:
+            level_rows.append(list(pre) + [int(mbr)])
+    rows = np.array(level_rows, np.int32)
+    sizes = np.array([len(g[1]) for g in groups], np.int32)
+    first = np.zeros(len(groups), np.int64)
+    first[1:] = np.cumsum(sizes)[:-1]
+    wg = np.array([4, 0, 2, 1, 3], np.int64)  # work entries in a different order than the groups
+    cnt = []
+    for g in wg:
+        mask = np.ones(n_words * 64, bool)
+        for c in groups[g][0]:
+            mask &= bits[c].astype(bool)
+        cnt.append(int(mask.sum()))
+    cnt = np.array(cnt, np.int64)
+    cl = eng.proj_stride(cnt, n_words)
+    m = sizes[wg].astype(np.int64)
+    cb = np.zeros(len(wg) + 1, np.int64)
+    np.cumsum(m * cl, out=cb[1:])
+    n_seg = -(-n_words // 1024)
+    d_fbv, d_rows = _dev(fbv_h.view(np.int64)), _dev(rows)
+    d_first, d_size, d_wg = _dev(first), _dev(sizes), _dev(wg)
+    seg_off = torch.full((len(wg) * (n_seg + 1),), -7, dtype=torch.int64, device="cuda")
+    out_words = torch.full((len(wg),), -7, dtype=torch.int64, device="cuda")
+    st = lib.etm_prefix_segments(d_fbv.data_ptr(), ld, n_words, d_rows.data_ptr(), width, d_first.data_ptr(),
+                                 d_wg.data_ptr(), len(wg), seg_off.data_ptr(), out_words.data_ptr(), _stream())
+    assert st == 0, lib.etm_last_error()
+    cbuf = torch.full((int(cb[-1]),), -1, dtype=torch.int64, device="cuda")
+    d_cbase, d_cld = _dev(cb[:-1].copy()), _dev(cl)
+    st = lib.etm_project(d_fbv.data_ptr(), ld, n_words, d_rows.data_ptr(), width, d_first.data_ptr(),
+                         d_size.data_ptr(), d_wg.data_ptr(), len(wg), seg_off.data_ptr(), d_cbase.data_ptr(),
+                         d_cld.data_ptr(), cbuf.data_ptr(), _stream())
+    assert st == 0, lib.etm_last_error()
+    got = cbuf.cpu().numpy().view(np.uint64)
+    want = _projection_reference(bits.astype(bool), ld, n_words, [groups[g] for g in wg], cl)
+    so = seg_off.cpu().numpy().reshape(len(wg), n_seg + 1)
+    ow = out_words.cpu().numpy()
+    for k in range(len(wg)):
+        seg_counts = [int(((np.logical_and.reduce([bits[c].astype(bool) for c in groups[wg[k]][0]]))
+                           [s * 65536:(s + 1) * 65536]).sum()) for s in range(n_seg)]
+        expect_off = np.concatenate([[0], np.cumsum([(c + 63) // 64 for c in seg_counts])])
+        assert np.array_equal(so[k], expect_off)
+        assert ow[k] == expect_off[-1] <= cl[k]
+        block = got[cb[k]:cb[k + 1]].reshape(m[k], cl[k])
+        assert np.array_equal(block, want[k]), f"work entry {k} (group {wg[k]})"
