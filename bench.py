@@ -274,7 +274,8 @@ def main() -> None:
     ap.add_argument("--serving-scale", type=float, default=1.0, help="serving: dataset row scale")
     ap.add_argument("--serving-requests", type=int, default=256)
     ap.add_argument("--method", default=None, choices=["popcount", "tensor"])
-    ap.add_argument("--tc-elem", type=int, default=1, choices=[1, 2], help="tensor operands: 1 = e4m3, 2 = f16")
+    ap.add_argument("--tc-elem", type=int, default=1, choices=[1, 2, 9, 10],
+                    help="tensor operands: 1 = e4m3, 2 = f16; + 8: the CTA-pair kernel")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparator")
     ap.add_argument("--proj-gb", type=float, default=4.0, help="device GB of projected words per chunk")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
@@ -422,7 +423,9 @@ def main() -> None:
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (hash-defined Bernoulli bits, on device)",
             "config": {"workload": args.workload, **spec, "method": method, "form": "batched",
-                       "tc_operands": ("e4m3" if args.tc_elem == 1 else "f16") if method == "tensor" else None,
+                       "tc_operands": (("e4m3" if args.tc_elem & 3 == 1 else "f16")
+                                       + (", CTA pairs (cta_group::2)" if args.tc_elem & 8 else ""))
+                       if method == "tensor" else None,
                        "l2": "inputs (1.02 GB of bitvectors) larger than L2; no flush",
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
             "levels": [{"k": s.k, "candidates": s.n_candidates, "frequent": s.n_frequent, "ms": round(s.ms, 2)}

@@ -478,6 +478,359 @@ int launch_gram(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cword
     return ETM_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// CTA-pair form (cta_group::2). A cluster of two CTAs on two SMs computes a 256 x 256 block pair
+// with one M = 256, N = 256 MMA per K step: CTA r holds A rows 128 r .. 128 r + 127 and B rows
+// 128 r .. 128 r + 127 of the blocks, the leader (rank 0) issues the MMAs and each CTA's tensor
+// memory receives its 128 A rows against all 256 B rows. Per SM and unit of MMA work this stages
+// 256 operand rows instead of 384 (128 on a diagonal block pair, where a CTA's A rows are its own
+// B rows) and the tensor cores read a third less shared memory.
+//
+// Hand-over: every producer warp of both CTAs arrives (one elected lane, cluster-scope release)
+// on the leader's full barrier of the stage; the leader's commits arrive on the empty and
+// accumulator barriers of both CTAs (multicast). Per block pair the two CTAs take the same
+// decisions (skip, abort) from values exchanged through distributed shared memory between
+// cluster barriers, so both always execute the same sequence of cluster barriers.
+//
+// Tensor memory: each CTA allocates PR_TMEM_COLS columns with cta_group::2 and the MMAs and both
+// epilogues use the leader's columns.
+//
+// Measured on GB300 (16 groups of 1,280 members over 131,072 projected rows): exact, but 3.3 ms
+// against 2.6 ms for gram_tc_kernel; without the operand stores it still takes 2.4 ms, so the pair's
+// cross-SM hand-over (remote arrivals, multicast commits) costs more than the shared-memory traffic it
+// saves. The engine keeps the single-CTA kernel by default; ETM_TC_PAIR selects this one.
+constexpr int PR_ROWS = 128;                     // A rows and B rows per CTA
+constexpr int PR_TILE = 256;                     // members per block
+constexpr int PR_STAGES = 6;
+constexpr int PR_PRODUCERS = 2 * PR_ROWS;        // thread t < 128: A row t; else B row t - 128
+constexpr int PR_PWARPS = PR_PRODUCERS / 32;
+constexpr int PR_THREADS = PR_PRODUCERS + 32;
+constexpr int PR_MMA_WARP = PR_PRODUCERS / 32;
+constexpr uint32_t PR_TMEM_COLS = 256;
+constexpr int PR_HALF = PR_ROWS * 128;           // bytes of one 128-row operand tile
+constexpr int PR_SLOT = 2 * PR_HALF;             // A tile, then B tile
+// + 1024 for the alignment of the slots, + one spare half tile after the last slot.
+constexpr int PR_SMEM = PR_STAGES * PR_SLOT + 1024 + PR_HALF;
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t map_to(uint32_t saddr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ uint32_t ld_cluster_u32(uint32_t caddr) {
+    uint32_t v;
+    asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(caddr) : "memory");
+    return v;
+}
+__device__ __forceinline__ void arrive_cluster(uint32_t caddr) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(caddr) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_cluster(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+    long long n = 0;
+    while (!mbar_try_cluster(bar, parity)) {
+        if (*abort_flag) return false;
+        if (++n > WAIT_LIMIT) {
+            *abort_flag = 1;
+            return false;
+        }
+    }
+    return true;
+}
+__device__ __forceinline__ void commit_pair(uint64_t* bar) {
+    asm volatile(
+        "{\n .reg .b16 msk;\n mov.b16 msk, 3;\n"
+        " tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], msk;\n}\n"
+        ::"r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void commit_pair_local(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+// Instruction descriptor of the pair MMA: D f32, A/B format code 0, K-major, N = 256, M = 256.
+__host__ __device__ constexpr uint32_t pair_desc() { return (1u << 4) | (256u >> 3) << 17 | (256u >> 4) << 24; }
+
+template <int ELEM>
+__device__ __forceinline__ void mma_pair(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc) {
+    if constexpr (ELEM == 2) {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(a), "l"(b), "r"(pair_desc()), "r"(acc));
+    } else {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(a), "l"(b), "r"(pair_desc()), "r"(acc));
+    }
+}
+
+template <int ELEM>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PR_THREADS, 1) gram_pair_kernel(
+    const uint64_t* __restrict__ src, const int64_t* __restrict__ cbase, const int64_t* __restrict__ cwords,
+    const int64_t* __restrict__ cld, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
+    const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
+    const uint8_t* __restrict__ cls, int32_t* __restrict__ out) {
+    constexpr int WORDS_PER_STAGE = ELEM == 2 ? 1 : 2;
+    extern __shared__ uint8_t dsmem[];
+    __shared__ __align__(8) uint64_t full_bar[PR_STAGES];   // the leader's: 2 x PR_PWARPS warp arrivals
+    __shared__ __align__(8) uint64_t empty_bar[PR_STAGES];  // each CTA's: the leader's commit
+    __shared__ __align__(8) uint64_t acc_bar;
+    __shared__ __align__(8) uint64_t drain_bar;
+    __shared__ uint32_t tmem_sh;
+    __shared__ int abort_sh;
+    __shared__ int any_sh[2];    // per block-pair parity: this CTA has a candidate to count
+    __shared__ int stop_sh[2];   // per block-pair parity: this CTA aborted
+    __shared__ int64_t off_a[PR_ROWS];
+    __shared__ int64_t off_b[PR_ROWS];
+
+    uint8_t* slots = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const uint32_t rank = cluster_rank();
+    const uint32_t peer = rank ^ 1u;
+
+    if (tid == 0) {
+        for (int s = 0; s < PR_STAGES; s++) {
+            mbar_init(&full_bar[s], 2 * PR_PWARPS);
+            mbar_init(&empty_bar[s], 1);
+        }
+        mbar_init(&acc_bar, 1);
+        mbar_init(&drain_bar, 1);
+        abort_sh = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == PR_MMA_WARP) {
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_sh)),
+                     "r"(PR_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+        tc_fence_before();
+    }
+    cluster_sync();
+    tc_fence_after();
+    const uint32_t tmem_own = tmem_sh;
+    const uint32_t tmem = rank == 0 ? tmem_own : ld_cluster_u32(map_to(smem_u32(&tmem_sh), 0));
+    volatile int* abort_flag = &abort_sh;
+
+    const int64_t total = work_off[n_work];
+    const int64_t pair = blockIdx.x >> 1, n_pairs = gridDim.x >> 1;
+    int64_t gstage = 0;
+    uint32_t tile_iter = 0;
+    int par = 0;
+    for (int64_t tp = pair; tp < total; tp += n_pairs, par ^= 1) {
+        const int64_t wi = upper_find(work_off, n_work, tp);
+        const int64_t g = work_groups[wi];
+        const int64_t m = grp_size[g];
+        const int64_t nb = ceil_div<int64_t>(m, PR_TILE);
+        int64_t ua, ub1;
+        tri_decode(tp - work_off[wi], nb + 1, &ua, &ub1);
+        const int64_t ub = ub1 - 1;
+        const bool diag = ua == ub;
+        const int64_t a0 = ua * PR_TILE + rank * PR_ROWS;  // this CTA's A rows
+        const int64_t b0 = ub * PR_TILE + rank * PR_ROWS;  // this CTA's B rows
+        const int64_t bcol0 = ub * PR_TILE;                // the accumulator's 256 columns
+        const int64_t cb = cand_off[g] - chunk_base;
+        const int64_t words = cwords[wi];
+        const int64_t n_stages = ceil_div<int64_t>(words, WORDS_PER_STAGE);
+        if (tid < PR_ROWS) {
+            const int64_t ia = a0 + tid, ib = b0 + tid;
+            off_a[tid] = ia < m ? cbase[wi] + ia * cld[wi] : -1;
+            off_b[tid] = ib < m ? cbase[wi] + ib * cld[wi] : -1;
+        }
+        int any = cls == nullptr;
+        if (!any && tid < PR_ROWS) {
+            const int64_t i = a0 + tid;
+            for (int c = 0; c < PR_TILE && !any; c++) {
+                const int64_t j = bcol0 + c;
+                any = i < j && j < m && cls[cb + tri_index(i, j, m)] == ETM_CAND_COUNT;
+            }
+        }
+        any = __syncthreads_or(any);
+        if (tid == 0) any_sh[par] = any;
+        cluster_sync();
+        const int pair_any = any | (int)ld_cluster_u32(map_to(smem_u32(&any_sh[par]), peer));
+        if (!pair_any) continue;  // both CTAs skip the block pair
+
+        if (warp < PR_MMA_WARP) {
+            // ---- producers: thread t expands A row t (t < 128) or B row t - 128 of this CTA ----
+            constexpr int PF = 4;
+            constexpr int BW = PF * WORDS_PER_STAGE;
+            const bool is_b = tid >= PR_ROWS;
+            const int prow = is_b ? tid - PR_ROWS : tid;
+            const bool idle = !is_b && diag;  // on a diagonal pair the A rows are this CTA's B rows
+            const int64_t off = idle ? -1 : (is_b ? off_b[prow] : off_a[prow]);
+            uint64_t cur[BW], nxt[BW];
+            auto load_batch = [&](int64_t s0, uint64_t* x) {
+#pragma unroll
+                for (int q = 0; q < BW; q += 2) {
+                    ulonglong2 v = make_ulonglong2(0, 0);
+                    if (off >= 0) v = __ldg(reinterpret_cast<const ulonglong2*>(src + off + s0 * WORDS_PER_STAGE + q));
+                    x[q] = v.x;
+                    x[q + 1] = v.y;
+                }
+            };
+            if (n_stages > 0) load_batch(0, cur);
+            for (int64_t s0 = 0; s0 < n_stages && !*abort_flag; s0 += PF) {
+                if (s0 + PF < n_stages) load_batch(s0 + PF, nxt);
+#pragma unroll
+                for (int j = 0; j < PF; j++) {
+                    const int64_t s = s0 + j;
+                    if (s >= n_stages) break;
+                    const int64_t G = gstage + s;
+                    const int slot = (int)(G % PR_STAGES);
+                    const uint32_t use = (uint32_t)(G / PR_STAGES);
+                    if (!mbar_wait(&empty_bar[slot], (use & 1u) ^ 1u, abort_flag)) break;
+                    if (!idle) {
+                        const uint64_t x0 = cur[j * WORDS_PER_STAGE];
+                        const uint64_t x1 = WORDS_PER_STAGE == 2 ? cur[j * WORDS_PER_STAGE + 1] : 0ULL;
+                        store_row<ELEM>(slots + slot * PR_SLOT + (is_b ? PR_HALF : 0), prow, x0, x1);
+                        fence_proxy_async();  // this CTA's tile, read by the pair's MMA through its own SM
+                    }
+                    __syncwarp();
+                    if (lane == 0) arrive_cluster(map_to(smem_u32(&full_bar[slot]), 0));
+                }
+#pragma unroll
+                for (int q = 0; q < BW; q++) cur[q] = nxt[q];
+            }
+            // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .., columns 128 (w / 4) .. +127 ----
+            const bool ok = n_stages == 0 || mbar_wait(&acc_bar, tile_iter & 1u, abort_flag);
+            if (ok) {
+                tc_fence_after();
+                const int lane_base = (warp & 3) * 32;
+                const int64_t i = a0 + lane_base + lane;
+                for (int q = 0; q < 4; q++) {
+                    const int col0 = (warp >> 2) * 128 + q * 32;
+                    uint32_t v[32];
+                    if (n_stages > 0) {
+                        const uint32_t taddr = tmem + ((uint32_t)lane_base << 16) + (uint32_t)col0;
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+                            "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                              "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+                              "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+                              "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                            : "r"(taddr));
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < 32; c++) v[c] = 0u;
+                    }
+                    if (i < m) {
+#pragma unroll
+                        for (int c = 0; c < 32; c++) {
+                            const int64_t j = bcol0 + col0 + c;
+                            if (i < j && j < m) {
+                                const int64_t t = cb + tri_index(i, j, m);
+                                if (cls == nullptr || cls[t] == ETM_CAND_COUNT)
+                                    out[t] = n_stages > 0 ? __float2int_rn(__uint_as_float(v[c]) * count_scale<ELEM>()) : 0;
+                            }
+                        }
+                    }
+                }
+            }
+            tc_fence_before();
+        } else if (rank == 0 && lane == 0) {
+            // ---- MMA issuer (the leader) ----
+            tc_fence_after();
+            for (int64_t s = 0; s < n_stages; s++) {
+                const int64_t G = gstage + s;
+                const int slot = (int)(G % PR_STAGES);
+                const uint32_t use = (uint32_t)(G / PR_STAGES);
+                if (!mbar_wait_cluster(&full_bar[slot], use & 1u, abort_flag)) break;
+                tc_fence_after();
+                const uint32_t base = smem_u32(slots + slot * PR_SLOT);
+                const uint32_t b_addr = base + PR_HALF;
+                const uint32_t a_addr = diag ? b_addr : base;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const uint32_t acc = (s > 0 || k > 0) ? 1u : 0u;
+                    mma_pair<ELEM>(tmem, smem_desc(a_addr + 32 * k), smem_desc(b_addr + 32 * k), acc);
+                }
+                commit_pair(&empty_bar[slot]);
+            }
+            commit_pair(&acc_bar);
+        }
+        gstage += n_stages;
+        tile_iter += 1;
+        __syncthreads();
+        if (tid == 0) stop_sh[par] = *abort_flag;
+        cluster_sync();  // the accumulator is read in both CTAs; both stop flags are set
+        const int stop = *abort_flag | (int)ld_cluster_u32(map_to(smem_u32(&stop_sh[par]), peer));
+        if (stop) {
+            *abort_flag = 1;
+            break;
+        }
+    }
+
+    // Teardown: the leader waits (bounded) for any MMA still in flight, then both CTAs free tensor memory.
+    if (rank == 0 && warp == PR_MMA_WARP && lane == 0 && *abort_flag) {
+        commit_pair_local(&drain_bar);
+        long long n = 0;
+        while (!mbar_test(&drain_bar, 0) && ++n < WAIT_LIMIT) __nanosleep(64);
+    }
+    __syncthreads();
+    cluster_sync();
+    if (warp == PR_MMA_WARP) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem_own), "r"(PR_TMEM_COLS)
+                     : "memory");
+    }
+    if (tid == 0 && *abort_flag) atomicExch(&g_tc_status, ETM_ETIMEOUT);
+}
+
+template <int ELEM>
+int launch_gram_pair(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
+                     const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
+                     const int64_t* work_off, int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls,
+                     int32_t* out, cudaStream_t s) {
+    static bool configured = false;
+    static int max_clusters = 0;
+    if (!configured) {
+        ETM_CUDA(cudaFuncSetAttribute(gram_pair_kernel<ELEM>, cudaFuncAttributeMaxDynamicSharedMemorySize, PR_SMEM));
+        // Persistent clusters: as many as can be resident at once (SM pairs within a GPC).
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(2 * max(1, sm_count() / 2));
+        cfg.blockDim = dim3(PR_THREADS);
+        cfg.dynamicSmemBytes = PR_SMEM;
+        cudaLaunchAttribute attr;
+        attr.id = cudaLaunchAttributeClusterDimension;
+        attr.val.clusterDim.x = 2;
+        attr.val.clusterDim.y = 1;
+        attr.val.clusterDim.z = 1;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        ETM_CUDA(cudaOccupancyMaxActiveClusters(&max_clusters, gram_pair_kernel<ELEM>, &cfg));
+        configured = true;
+    }
+    const int64_t pairs = max(1, min(max_clusters, sm_count() / 2));
+    const int grid = 2 * (int)max64(1, min64(pairs, n_tiles > 0 ? n_tiles : pairs));
+    gram_pair_kernel<ELEM><<<grid, PR_THREADS, PR_SMEM, s>>>(cbuf, cbase, cwords, cld, grp_size, cand_off,
+                                                             work_groups, work_off, n_work, chunk_base, cls, out);
+    ETM_LAUNCHED("gram_tc");
+    return ETM_OK;
+}
+
 }  // namespace
 
 namespace etm {
@@ -487,11 +840,14 @@ int gram_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, c
             int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t elem, int32_t* out,
             cudaStream_t s) {
     // elem: 1 = e4m3, 2 = f16; + ETM_TC_A_TMEM: the A operand is staged in tensor memory
-    // (tcgen05.st) instead of shared memory.
+    // (tcgen05.st) instead of shared memory; + ETM_TC_PAIR: the CTA-pair kernel (cta_group::2).
     const bool a_tmem = (elem & ETM_TC_A_TMEM) != 0;
-    const int e = elem & ~ETM_TC_A_TMEM;
+    const bool pair = (elem & ETM_TC_PAIR) != 0;
+    const int e = elem & ~(ETM_TC_A_TMEM | ETM_TC_PAIR);
     ETM_REQUIRE(e == 1 || e == 2, ETM_EINVAL, "gram_tc: element code %d (1 = e4m3, 2 = f16)", e);
+    ETM_REQUIRE(!(pair && a_tmem), ETM_EINVAL, "gram_tc: the CTA-pair form stages both operands in shared memory");
 #define ETM_GRAM_ARGS cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, n_tiles, chunk_base, cls, out, s
+    if (pair) return e == 2 ? launch_gram_pair<2>(ETM_GRAM_ARGS) : launch_gram_pair<1>(ETM_GRAM_ARGS);
     if (e == 2) return a_tmem ? launch_gram<2, true>(ETM_GRAM_ARGS) : launch_gram<2, false>(ETM_GRAM_ARGS);
     return a_tmem ? launch_gram<1, true>(ETM_GRAM_ARGS) : launch_gram<1, false>(ETM_GRAM_ARGS);
 #undef ETM_GRAM_ARGS

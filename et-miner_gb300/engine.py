@@ -78,11 +78,15 @@ def proj_stride(pcnt: np.ndarray, n_words: int) -> np.ndarray:
     return np.maximum(32, ((np.asarray(pcnt, np.int64) + 63) // 64 + n_seg + 31) // 32 * 32)
 
 
-def _tile_items(m: np.ndarray, method: int) -> np.ndarray:
-    """Work items of groups of m members: 64 x 64 tile-pairs (popcount) or 128 x 256 Gram items (tensor)."""
+TC_PAIR = 8  # ETM_TC_PAIR: the CTA-pair Gram kernel (tc_elem flag)
+
+
+def _tile_items(m: np.ndarray, method: int, tc_elem: int = 1) -> np.ndarray:
+    """Work items of groups of m members: 64 x 64 tile-pairs (popcount), 128 x 256 Gram items (tensor)
+    or 256 x 256 block pairs (tensor, CTA-pair kernel)."""
     if method == 1:
         nb = (m + TC_TILE - 1) // TC_TILE
-        return nb * (nb + 1)
+        return nb * (nb + 1) // 2 if tc_elem & TC_PAIR else nb * (nb + 1)
     nt = (m + TILE - 1) // TILE
     return nt * (nt + 1) // 2
 
@@ -342,7 +346,7 @@ class Engine:
         cb = np.zeros(len(gids) + 1, np.int64)
         np.cumsum(m * cl, out=cb[1:])
         toff = np.zeros(len(gids) + 1, np.int64)
-        np.cumsum(_tile_items(m, method), out=toff[1:])
+        np.cumsum(_tile_items(m, method, self.tc_elem), out=toff[1:])
         n = len(gids)
         # cwords starts as the bound (whole words of the prefix rows plus one padded word per segment);
         # etm_prefix_segments overwrites it with the exact padded length.
@@ -583,7 +587,7 @@ class Engine:
                 if kind == "tiles" and whole_tc:
                     mg = sizes[gids]
                     toff = np.zeros(len(gids) + 1, np.int64)
-                    np.cumsum(_tile_items(mg, 1), out=toff[1:])
+                    np.cumsum(_tile_items(mg, 1, self.tc_elem), out=toff[1:])
                     n = len(gids)
                     host = np.concatenate([gids, toff, np.zeros(n, np.int64), np.full(n, n_words, np.int64),
                                            np.full(n, ldp, np.int64)])

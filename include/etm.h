@@ -54,6 +54,10 @@ extern "C" {
 /* Flag added to etm_count_tiles_tc's elem: stage the A operand in tensor memory (tcgen05.st)
  * instead of shared memory. Exact either way; the shared-memory form is faster on GB300. */
 #define ETM_TC_A_TMEM 4
+/* Flag added to etm_count_tiles_tc's elem: the CTA-pair kernel (two SMs per 256 x 256 block pair,
+ * tcgen05 cta_group::2); its work offsets count C(nb + 1, 2) block pairs per group (nb = ceil(m/256))
+ * instead of nb (nb + 1) half tiles. */
+#define ETM_TC_PAIR 8
 
 /* Rows of one projection segment: 1024 bitvector words (65,536 transactions). */
 #define ETM_PROJ_SEG_WORDS 1024
