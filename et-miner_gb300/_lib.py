@@ -96,6 +96,8 @@ SIGNATURES: dict[str, tuple] = {
     "etm_classify": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _P, _P, _I64, _I64, _I32, _P, _P, _P]),
     "etm_count_tiles": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P]),
     "etm_count_cands": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _P, _P]),
+    "etm_triple_counts_rows": (ctypes.c_int, [_P, _P, _I64, _P, _I64, _I64, _P, _P, _I64, _P, _P, _P, _I64, _I64, _P,
+                                              _P, _P]),
     "etm_pair_counts_rows": (ctypes.c_int, [_P, _P, _I64, _P, _I64, _I64, _I64, _P, _P]),
     "etm_prefix_counts": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _I64, _P, _P]),
     "etm_prefix_rows": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _I64, _P, _P, _P]),

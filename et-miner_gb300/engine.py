@@ -56,6 +56,9 @@ TC_MAX_ROWS = 1 << 24
 PROJ_SEG_WORDS = 1024  # ETM_PROJ_SEG_WORDS: bitvector words per projection segment
 #: Row-wise K=2 crossover: rows' pair increments over pairs x words (the reference's K2_ROWS_MAX_R).
 K2_ROWS_MAX_R = 3.95e-3
+#: Row-wise K=3 crossover: rows' pair increments over K=3 candidates x words, with every candidate in one
+#: chunk (the reference's K3_ROWS_MAX_R, gpu/row_split_chunks.py:145-159).
+K3_ROWS_MAX_R = 2.5e-4
 #: Counting method for tile-pairs: "popcount" or "tensor".
 DEFAULT_METHOD = "tensor"
 
@@ -125,6 +128,7 @@ class LevelStats:
     n_groups: int = 0
     n_chunks: int = 0
     launches: int = 0
+    row_wise: bool = False  # counted from the transactions (row-wise K=2 / K=3 kernels)
 
 
 @dataclass
@@ -239,7 +243,10 @@ class Engine:
         #: K=2 counts row-wise from the transactions (when given) while
         #: sum C(len,2) / (pairs x words) is below this (gpu/row_split_chunks.py:130-142); 0 disables.
         self.k2_rows_max_r = K2_ROWS_MAX_R
+        self.k3_rows_max_r = K3_ROWS_MAX_R
         self._k2_rows = None
+        self._rows_input = None
+        self._rows_input = None
         #: Counting settings chosen per level shape by timing (None: the fixed defaults).
         self.autotuner = Autotuner() if autotune is True else (autotune or None)
         self.scratch = _Scratch(self.device)
@@ -486,7 +493,12 @@ class Engine:
         tensor = self.method == "tensor"
         pcnt = np.zeros(G, np.int64)
         proj = np.zeros(G, bool)
-        if (self.project or tensor) and width >= 2 and big.any():
+        ri = self._rows_input
+        # K=3 from the transactions: each row adds 1 to the candidates it holds (sparse rows, one chunk).
+        k3_rows = (width == 2 and ri is not None and self.k3_rows_max_r > 0 and total <= self.chunk_cands
+                   and ri["pair_work"] < self.k3_rows_max_r * total * n_words)
+        stats.row_wise = stats.row_wise or k3_rows
+        if not k3_rows and (self.project or tensor) and width >= 2 and big.any():
             ids_big = np.flatnonzero(big)
             pcnt[ids_big] = self.prefix_counts(fbv, ldp, n_words, gen, grp_first, ids_big)
             if tensor:
@@ -546,6 +558,7 @@ class Engine:
             start_ev.record(main)
             side.wait_event(start_ev)  # the generating level and group tables come from the main stream
             prep(0)
+        grp_of = None
         for c, (g0, g1) in enumerate(chunks):
             base = int(offs[g0])
             n_c = int(offs[g1] - base)
@@ -562,6 +575,7 @@ class Engine:
             pr = proj[g0:g1]
             k2_rows = width == 1 and self._k2_rows is not None
             if k2_rows:
+                stats.row_wise = True
                 # K=2 from the transactions (one group of every generator): pair counts by row-wise increments.
                 rp, cl, nnz, lut, n_r = self._k2_rows
                 n_g = int(sizes[0])
@@ -569,7 +583,19 @@ class Engine:
                     _p(rp), _p(cl), nnz, _p(lut), lut.numel(), n_r, n_g, _p(counts), _stream()))
                 check(st, "etm_pair_counts_rows")
                 self.launches += 1
-            for kind, sel in (() if k2_rows else (("cands", small), ("tiles", ~small & ~pr), ("proj", pr & ~small))):
+            if k3_rows:
+                if grp_of is None:
+                    grp_of = torch.full((ri["ng"],), -1, dtype=torch.int32, device=self.device)
+                    grp_of[gen.rows[grp_first[:G], 0].long()] = torch.arange(G, dtype=torch.int32, device=self.device)
+                st = self._launch("triple_counts_rows", ri["nnz"] * 8 + ri["n_r"] * 8 + n_c * 4,
+                                  lambda: self.lib.etm_triple_counts_rows(
+                                      _p(ri["rp"]), _p(ri["cl"]), ri["nnz"], _p(ri["lut"]), ri["lut"].numel(),
+                                      ri["n_r"], _p(gen.rows), _p(grp_of), ri["ng"], _p(grp_first), _p(grp_size),
+                                      _p(cand_off), base, n_c, _p(cls), _p(counts), _stream()))
+                check(st, "etm_triple_counts_rows")
+                self.launches += 2
+            for kind, sel in (() if (k2_rows or k3_rows) else
+                              (("cands", small), ("tiles", ~small & ~pr), ("proj", pr & ~small))):
                 gids = ids[sel]
                 if len(gids) == 0:
                     continue
@@ -684,6 +710,7 @@ class Engine:
         against the pair space (the reference's rule, gpu/row_split_chunks.py:124-142)."""
         ptr, (n_cols, ld), _owner = as_device_bitvecs(bitvecs)
         self._k2_rows = None
+        self._rows_input = None
         if n_rows >= 2**31:
             raise ValueError(f"n_transactions={n_rows:,} exceeds int32 max: the count arrays are int32")
         n_words = (n_rows + 63) // 64
@@ -708,14 +735,16 @@ class Engine:
             return out
         fbv, ldp = self.gather(ptr, ld, gen_cols, n_words)
         ng = len(gen_cols)
-        if rows is not None and self.k2_rows_max_r > 0:
+        if rows is not None:
             rp, cl, lens = rows
             pair_work = float((lens.astype(np.float64) * (lens - 1) / 2).sum())
+            lut = torch.full((max(1, n_cols),), -1, dtype=torch.int32, device=self.device)
+            lut[torch.from_numpy(gen_cols.astype(np.int64)).to(self.device)] = torch.arange(
+                ng, dtype=torch.int32, device=self.device)
+            self._rows_input = dict(rp=rp, cl=cl, nnz=int(cl.numel()), lut=lut, n_r=int(rp.numel()) - 1,
+                                    pair_work=pair_work, ng=ng)
             r = pair_work / max(1.0, ng * (ng - 1) / 2 * n_words)
-            if r < self.k2_rows_max_r:
-                lut = torch.full((max(1, n_cols),), -1, dtype=torch.int32, device=self.device)
-                lut[torch.from_numpy(gen_cols.astype(np.int64)).to(self.device)] = torch.arange(
-                    ng, dtype=torch.int32, device=self.device)
+            if self.k2_rows_max_r > 0 and r < self.k2_rows_max_r:
                 self._k2_rows = (rp, cl, int(cl.numel()), lut, int(rp.numel()) - 1)
         gen = Level(torch.arange(ng, dtype=torch.int32, device=self.device)[:, None].contiguous(),
                     torch.from_numpy(col_counts[gen_cols].astype(np.int32)).to(self.device),

@@ -173,6 +173,24 @@ int etm_pair_counts_rows(const int64_t* row_ptr, const int32_t* cols, int64_t nn
                          int64_t lut_size, int64_t n_rows, int64_t n_gen, int32_t* out_counts, void* stream);
 
 /*
+ * Row-wise K=3 counts (count_k3_rows, gpu/kernels/_src/k3_rows.cu:50-140; chosen by the reference when
+ * r3 = sum over rows of C(len, 2) / (K=3 candidates x words) < 2.5e-4 and every candidate fits one chunk,
+ * gpu/row_split_chunks.py:145-159). The candidates are those of the prefix groups of a width-2 generating
+ * level: gen_rows int32 [n][2] (generator indices, lexsorted), group g = rows [grp_first[g],
+ * grp_first[g] + grp_size[g]) sharing item gen_rows[grp_first[g]][0], candidate (u, v_i, v_j) at
+ * cand_off[g] + tri_index(i, j, grp_size[g]); grp_of int32 [n_gen1] maps a generator to the group it
+ * prefixes or -1. out_counts int32 [n_cands] holds candidates [chunk_base, chunk_base + n_cands): those
+ * whose class is ETM_CAND_COUNT (all when cls is NULL) are zeroed, then each row adds 1 to every one of
+ * them whose three items it holds; the others are left as they were. row_ptr / cols / lut as for
+ * etm_pair_counts_rows.
+ */
+int etm_triple_counts_rows(const int64_t* row_ptr, const int32_t* cols, int64_t nnz, const int32_t* lut,
+                           int64_t lut_size, int64_t n_rows, const int32_t* gen_rows, const int32_t* grp_of,
+                           int64_t n_gen1, const int64_t* grp_first, const int32_t* grp_size,
+                           const int64_t* cand_off, int64_t chunk_base, int64_t n_cands, const uint8_t* cls,
+                           int32_t* out_counts, void* stream);
+
+/*
  * Prefix projection (the reference's projection counting of wide groups,
  * core/cpu_miner.py:720-791, on the device). For the listed groups (width >= 2):
  *   etm_prefix_counts  out_counts int64 [n_work] = rows holding the group's prefix

@@ -20,9 +20,11 @@ pytestmark = pytest.mark.gpu
 CASES = [c["name"] for c in json.loads((Path(__file__).parent / "golden" / "cases.json").read_text())["cases"]]
 
 
-def _rows_engine(e):
-    """An engine that counts K=2 row-wise whenever the transactions are given."""
+def _rows_engine(e, k3=False):
+    """An engine that counts K=2 (and with ``k3`` K=3) row-wise whenever the transactions are given."""
     e.k2_rows_max_r = float("inf")
+    if k3:
+        e.k3_rows_max_r = float("inf")
     return e
 
 
@@ -39,6 +41,7 @@ def engines(pkg):
         "noproj": eng.Engine(form="batched", project=False),
         "popcount": eng.Engine(method="popcount"),
         "rows": _rows_engine(eng.Engine()),
+        "rows3": _rows_engine(eng.Engine(), k3=True),
         "tuned": eng.Engine(autotune=import_module(pkg.__name__ + ".autotune").Autotuner(min_candidates=1)),
     }
 
@@ -58,7 +61,7 @@ def test_transactions_match_golden(pkg, golden_cases, engines, name):
         assert pairs == want
 
 
-@pytest.mark.parametrize("form", ["plain", "tiny", "proj", "noproj", "popcount", "tuned", "rows"])
+@pytest.mark.parametrize("form", ["plain", "tiny", "proj", "noproj", "popcount", "tuned", "rows", "rows3"])
 @pytest.mark.parametrize("name", ["implication_plain", "implication_prune", "implication_infer", "plain_small_plain",
                                   "deep_sparse_small", "dense_k2_small", "word_tail_65"])
 def test_forms_match_golden(pkg, golden_cases, engines, name, form):
@@ -167,3 +170,25 @@ def test_level_callback_and_profile(pkg):
     assert [c[0] for c in calls] == [1, 2, 3]
     assert [c[2] for c in calls] == [5, 7, 3]
     assert [p.name for p in session.phases] == ["k1", "k2", "k3"]
+
+
+def test_row_wise_k3_is_used_and_exact(pkg, golden_cases):
+    """The transactions route with the K=3 crossover forced: level 3 is counted row-wise and every level
+    equals the bitvector route's."""
+    from importlib import import_module
+
+    import torch
+
+    engm = import_module(pkg.__name__ + ".engine")
+    api = import_module(pkg.__name__ + ".api")
+    case = golden_cases["deep_sparse_small"]
+    indptr, items, n_rows = case_input(pkg, case)
+    n_cols = int(items.max()) + 1
+    bv, rows = api.build_device_bitvecs(indptr, items.astype(np.int32), n_cols, n_rows, keep_rows=True)
+    e = _rows_engine(engm.Engine(), k3=True)
+    got = e.mine(bv.view(torch.uint64), n_rows, case["min_support"], max_length=case["max_length"], rows=rows)
+    assert len(got.stats) >= 3 and got.stats[2].row_wise
+    ref = engm.Engine().mine(bv.view(torch.uint64), n_rows, case["min_support"], max_length=case["max_length"])
+    assert len(got.levels) == len(ref.levels)
+    for a, b in zip(got.levels, ref.levels):
+        assert torch.equal(a.rows, b.rows) and torch.equal(a.counts, b.counts)

@@ -369,3 +369,65 @@ def test_segmented_projection(pkg, lib, n_words, width):
         assert ow[k] == expect_off[-1] <= cl[k]
         block = got[cb[k]:cb[k + 1]].reshape(m[k], cl[k])
         assert np.array_equal(block, want[k]), f"work entry {k} (group {wg[k]})"
+
+
+@pytest.mark.parametrize("long_rows", [False, True])
+def test_triple_counts_rows_match_host(pkg, lib, long_rows):
+    """Row-wise K=3 (k3_rows.cu:50-140 restated on the prefix-group layout): the counts of a candidate range
+    from the rows, only for candidates classed as counted; the other classes keep their values."""
+    import torch
+
+    rng = np.random.default_rng(7 + long_rows)
+    n_rows, n_cols = 2500, 700 if long_rows else 120
+    lens = rng.integers(0, 14, n_rows)
+    if long_rows:
+        lens[::211] = 600  # beyond the 512-entry shared slice
+    rows = [np.sort(rng.choice(n_cols, size=min(l, n_cols), replace=False)) for l in lens]
+    indptr = np.zeros(n_rows + 1, np.int64)
+    np.cumsum([len(r) for r in rows], out=indptr[1:])
+    cols = np.concatenate(rows).astype(np.int32)
+    gen = np.flatnonzero(rng.random(n_cols) < 0.8)  # columns that generate
+    lut = np.full(n_cols, -1, np.int32)
+    lut[gen] = np.arange(len(gen), dtype=np.int32)
+    ng = len(gen)
+    # A K=2 generating level: a random set of pairs (u < v) of generator indices, lexsorted.
+    iu, iv = np.triu_indices(ng, 1)
+    keep = rng.random(len(iu)) < (0.05 if long_rows else 0.3)
+    pairs = np.stack([iu[keep], iv[keep]], 1).astype(np.int32)
+    us, starts, counts = np.unique(pairs[:, 0], return_index=True, return_counts=True)
+    sel = counts >= 2
+    us, starts, counts = us[sel], starts[sel], counts[sel]
+    G = len(us)
+    cand = counts.astype(np.int64) * (counts - 1) // 2
+    cand_off = np.zeros(G + 1, np.int64)
+    np.cumsum(cand, out=cand_off[1:])
+    grp_of = np.full(ng, -1, np.int32)
+    grp_of[us] = np.arange(G, dtype=np.int32)
+    total = int(cand_off[-1])
+    want = np.zeros(total, np.int64)
+    for r in rows:
+        g = lut[r]
+        g = g[g >= 0]
+        for a, u in enumerate(g):
+            k = grp_of[u]
+            if k < 0:
+                continue
+            mem = pairs[starts[k]:starts[k] + counts[k], 1]
+            idx = np.searchsorted(mem, g[a + 1:])
+            ok = (idx < len(mem)) & (mem[np.minimum(idx, len(mem) - 1)] == g[a + 1:])
+            idx = idx[ok]
+            ii, jj = np.triu_indices(len(idx), 1)
+            m = counts[k]
+            t = cand_off[k] + idx[ii] * (2 * m - idx[ii] - 1) // 2 + (idx[jj] - idx[ii] - 1)
+            np.add.at(want, t, 1)
+    base, n_c = total // 5, total - total // 5 - 3
+    cls = rng.integers(0, 3, n_c).astype(np.uint8)  # 0 counted; other classes keep their values
+    expect = np.where(cls == 0, want[base:base + n_c], -7)
+    out = torch.full((n_c,), -7, dtype=torch.int32, device="cuda")
+    d = [_dev(indptr), _dev(cols), _dev(lut), _dev(pairs), _dev(grp_of), _dev(starts.astype(np.int64)),
+         _dev(counts.astype(np.int32)), _dev(cand_off), _dev(cls)]
+    st = lib.etm_triple_counts_rows(d[0].data_ptr(), d[1].data_ptr(), len(cols), d[2].data_ptr(), n_cols, n_rows,
+                                    d[3].data_ptr(), d[4].data_ptr(), ng, d[5].data_ptr(), d[6].data_ptr(),
+                                    d[7].data_ptr(), base, n_c, d[8].data_ptr(), out.data_ptr(), _stream())
+    assert st == 0, lib.etm_last_error()
+    assert np.array_equal(out.cpu().numpy(), expect)
