@@ -274,8 +274,8 @@ def main() -> None:
     ap.add_argument("--serving-scale", type=float, default=1.0, help="serving: dataset row scale")
     ap.add_argument("--serving-requests", type=int, default=256)
     ap.add_argument("--method", default=None, choices=["popcount", "tensor"])
-    ap.add_argument("--tc-elem", type=int, default=1, choices=[1, 2, 9, 10],
-                    help="tensor operands: 1 = e4m3, 2 = f16; + 8: the CTA-pair kernel")
+    ap.add_argument("--tc-elem", type=int, default=17, choices=[1, 2, 9, 10, 17, 18],
+                    help="tensor operands: 1 = e4m3, 2 = f16; + 8: the CTA-pair kernel; + 16: the 256 x 256 kernel")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparator")
     ap.add_argument("--proj-gb", type=float, default=4.0, help="device GB of projected words per chunk")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
@@ -395,7 +395,7 @@ def main() -> None:
         per_launch_s = top["ms"] / top["launches"] / 1e3
         if top["name"] == "gram_tc":
             # Useful work: 2 x C(m,2) x rows per group; the e4m3 MMAs run at twice the dense bf16 rate.
-            fp8 = method == "tensor" and eng.tc_elem == 1
+            fp8 = method == "tensor" and eng.tc_elem & 3 == 1
             peak = peaks["bf16_tflops"] * (2.0 if fp8 else 1.0)
             achieved = top["flops"] / top["launches"] / per_launch_s / 1e12
             roof = {"bound": "tensor", "kernel": top["name"], "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
@@ -424,7 +424,8 @@ def main() -> None:
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (hash-defined Bernoulli bits, on device)",
             "config": {"workload": args.workload, **spec, "method": method, "form": "batched",
                        "tc_operands": (("e4m3" if args.tc_elem & 3 == 1 else "f16")
-                                       + (", CTA pairs (cta_group::2)" if args.tc_elem & 8 else ""))
+                                       + (", CTA pairs (cta_group::2)" if args.tc_elem & 8 else "")
+                                       + (", 256 x 256 tiles" if args.tc_elem & 16 else ", 128 x 256 tiles"))
                        if method == "tensor" else None,
                        "l2": "inputs (1.02 GB of bitvectors) larger than L2; no flush",
                        "parallelism": "replicas" if world > 1 else "1 GPU"},

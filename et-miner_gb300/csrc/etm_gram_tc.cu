@@ -479,6 +479,237 @@ int launch_gram(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cword
 }
 
 // ---------------------------------------------------------------------------------------------
+// Wide form: one CTA computes a whole 256 x 256 block pair with two M = 128 MMAs per K step that
+// share the B tile (accumulators in TMEM columns 0-255 and 256-511). Per stage it stages 512
+// operand rows (256 on a diagonal block pair) for twice the MMA work of a 128 x 256 item: a third
+// fewer shared-memory stores per unit of work than gram_tc_kernel.
+constexpr int WD_TILE = 256;                     // A rows and B rows per block pair
+constexpr int WD_STAGES = 3;
+constexpr int WD_PRODUCERS = 2 * WD_TILE;        // thread t < 256: A row t; else B row t - 256
+constexpr int WD_THREADS = WD_PRODUCERS + 32;
+constexpr int WD_MMA_WARP = WD_PRODUCERS / 32;
+constexpr int WD_HALF = 128 * 128;               // bytes of one 128-row operand tile
+constexpr int WD_SLOT = 4 * WD_HALF;             // A (two halves), then B (two halves)
+constexpr int WD_SMEM = WD_STAGES * WD_SLOT + 1024;
+
+template <int ELEM>
+__global__ void __launch_bounds__(WD_THREADS, 1) gram_wide_kernel(
+    const uint64_t* __restrict__ src, const int64_t* __restrict__ cbase, const int64_t* __restrict__ cwords,
+    const int64_t* __restrict__ cld, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
+    const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
+    const uint8_t* __restrict__ cls, int32_t* __restrict__ out) {
+    constexpr int WORDS_PER_STAGE = ELEM == 2 ? 1 : 2;
+    extern __shared__ uint8_t dsmem[];
+    __shared__ __align__(8) uint64_t full_bar[WD_STAGES];
+    __shared__ __align__(8) uint64_t empty_bar[WD_STAGES];
+    __shared__ __align__(8) uint64_t acc_bar;
+    __shared__ __align__(8) uint64_t drain_bar;
+    __shared__ uint32_t tmem_sh;
+    __shared__ int abort_sh;
+    __shared__ int64_t off_a[WD_TILE];
+    __shared__ int64_t off_b[WD_TILE];
+
+    uint8_t* slots = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) {
+        for (int s = 0; s < WD_STAGES; s++) {
+            mbar_init(&full_bar[s], WD_PRODUCERS);
+            mbar_init(&empty_bar[s], 1);
+        }
+        mbar_init(&acc_bar, 1);
+        mbar_init(&drain_bar, 1);
+        abort_sh = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == WD_MMA_WARP) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_sh)),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        tc_fence_before();
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_sh;
+    volatile int* abort_flag = &abort_sh;
+
+    const int64_t total = work_off[n_work];
+    int64_t gstage = 0;
+    uint32_t tile_iter = 0;
+    for (int64_t tp = blockIdx.x; tp < total; tp += gridDim.x) {
+        const int64_t wi = upper_find(work_off, n_work, tp);
+        const int64_t g = work_groups[wi];
+        const int64_t m = grp_size[g];
+        const int64_t nb = ceil_div<int64_t>(m, WD_TILE);
+        int64_t ua, ub1;
+        tri_decode(tp - work_off[wi], nb + 1, &ua, &ub1);
+        const int64_t ub = ub1 - 1;
+        const bool diag = ua == ub;
+        const int64_t a0 = ua * WD_TILE, b0 = ub * WD_TILE;
+        const int64_t cb = cand_off[g] - chunk_base;
+        const int64_t words = cwords[wi];
+        const int64_t n_stages = ceil_div<int64_t>(words, WORDS_PER_STAGE);
+        if (tid < WD_TILE) {
+            const int64_t ia = a0 + tid, ib = b0 + tid;
+            off_a[tid] = ia < m ? cbase[wi] + ia * cld[wi] : -1;
+            off_b[tid] = ib < m ? cbase[wi] + ib * cld[wi] : -1;
+        }
+        int any = cls == nullptr;
+        if (!any && tid < WD_TILE) {
+            const int64_t i = a0 + tid;
+            for (int c = 0; c < WD_TILE && !any; c++) {
+                const int64_t j = b0 + c;
+                any = i < j && j < m && cls[cb + tri_index(i, j, m)] == ETM_CAND_COUNT;
+            }
+        }
+        if (!__syncthreads_or(any)) continue;
+
+        if (warp < WD_MMA_WARP) {
+            // ---- producers: thread t expands A row t (t < 256) or B row t - 256 ----
+            constexpr int PF = 4;
+            constexpr int BW = PF * WORDS_PER_STAGE;
+            const bool is_b = tid >= WD_TILE;
+            const int prow = is_b ? tid - WD_TILE : tid;
+            const bool idle = !is_b && diag;  // on a diagonal block pair the A rows are the B rows
+            const int64_t off = idle ? -1 : (is_b ? off_b[prow] : off_a[prow]);
+            // Row r of a 256-row operand: half r / 128 (16 KB apart), row r % 128 of the half.
+            const int dst = (is_b ? 2 * WD_HALF : 0) + (prow >> 7) * WD_HALF;
+            const int hrow = prow & 127;
+            uint64_t cur[BW], nxt[BW];
+            auto load_batch = [&](int64_t s0, uint64_t* x) {
+#pragma unroll
+                for (int q = 0; q < BW; q += 2) {
+                    ulonglong2 v = make_ulonglong2(0, 0);
+                    if (off >= 0) v = __ldg(reinterpret_cast<const ulonglong2*>(src + off + s0 * WORDS_PER_STAGE + q));
+                    x[q] = v.x;
+                    x[q + 1] = v.y;
+                }
+            };
+            if (n_stages > 0) load_batch(0, cur);
+            for (int64_t s0 = 0; s0 < n_stages && !*abort_flag; s0 += PF) {
+                if (s0 + PF < n_stages) load_batch(s0 + PF, nxt);
+#pragma unroll
+                for (int j = 0; j < PF; j++) {
+                    const int64_t s = s0 + j;
+                    if (s >= n_stages) break;
+                    const int64_t G = gstage + s;
+                    const int slot = (int)(G % WD_STAGES);
+                    const uint32_t use = (uint32_t)(G / WD_STAGES);
+                    if (!mbar_wait(&empty_bar[slot], (use & 1u) ^ 1u, abort_flag)) break;
+                    if (!idle) {
+                        const uint64_t x0 = cur[j * WORDS_PER_STAGE];
+                        const uint64_t x1 = WORDS_PER_STAGE == 2 ? cur[j * WORDS_PER_STAGE + 1] : 0ULL;
+                        store_row<ELEM>(slots + slot * WD_SLOT + dst, hrow, x0, x1);
+                        fence_proxy_async();
+                    }
+                    mbar_arrive(&full_bar[slot]);
+                }
+#pragma unroll
+                for (int q = 0; q < BW; q++) cur[q] = nxt[q];
+            }
+            // ---- epilogue: warp w reads lanes 32 (w % 4) .. of accumulator (w / 8), columns 128 ((w / 4) % 2) .. ----
+            const bool ok = n_stages == 0 || mbar_wait(&acc_bar, tile_iter & 1u, abort_flag);
+            if (ok) {
+                tc_fence_after();
+                const int lane_base = (warp & 3) * 32;
+                const int accn = warp >> 3;
+                const int64_t i = a0 + accn * 128 + lane_base + lane;
+                for (int q = 0; q < 4; q++) {
+                    const int col0 = ((warp >> 2) & 1) * 128 + q * 32;
+                    uint32_t v[32];
+                    if (n_stages > 0) {
+                        const uint32_t taddr = tmem + ((uint32_t)lane_base << 16) + (uint32_t)(accn * 256 + col0);
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+                            "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                              "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+                              "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+                              "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                            : "r"(taddr));
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < 32; c++) v[c] = 0u;
+                    }
+                    if (i < m) {
+#pragma unroll
+                        for (int c = 0; c < 32; c++) {
+                            const int64_t j = b0 + col0 + c;
+                            if (i < j && j < m) {
+                                const int64_t t = cb + tri_index(i, j, m);
+                                if (cls == nullptr || cls[t] == ETM_CAND_COUNT)
+                                    out[t] = n_stages > 0 ? __float2int_rn(__uint_as_float(v[c]) * count_scale<ELEM>()) : 0;
+                            }
+                        }
+                    }
+                }
+            }
+            tc_fence_before();
+        } else if (lane == 0) {
+            // ---- MMA issuer: two M = 128 MMAs per K step, sharing the B tile ----
+            tc_fence_after();
+            for (int64_t s = 0; s < n_stages; s++) {
+                const int64_t G = gstage + s;
+                const int slot = (int)(G % WD_STAGES);
+                const uint32_t use = (uint32_t)(G / WD_STAGES);
+                if (!mbar_wait(&full_bar[slot], use & 1u, abort_flag)) break;
+                tc_fence_after();
+                const uint32_t base = smem_u32(slots + slot * WD_SLOT);
+                const uint32_t b_addr = base + 2 * WD_HALF;
+                const uint32_t a_addr = diag ? b_addr : base;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const uint32_t acc = (s > 0 || k > 0) ? 1u : 0u;
+                    const uint64_t bd = smem_desc(b_addr + 32 * k);
+                    mma_ss<ELEM>(tmem, smem_desc(a_addr + 32 * k), bd, acc);
+                    mma_ss<ELEM>(tmem + 256, smem_desc(a_addr + WD_HALF + 32 * k), bd, acc);
+                }
+                mma_commit(&empty_bar[slot]);
+            }
+            mma_commit(&acc_bar);
+        }
+        gstage += n_stages;
+        tile_iter += 1;
+        __syncthreads();
+        if (*abort_flag) break;
+    }
+
+    if (warp == WD_MMA_WARP) {
+        if (lane == 0 && *abort_flag) {
+            mma_commit(&drain_bar);
+            long long n = 0;
+            while (!mbar_test(&drain_bar, 0) && ++n < WAIT_LIMIT) __nanosleep(64);
+        }
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+    }
+    if (tid == 0 && *abort_flag) atomicExch(&g_tc_status, ETM_ETIMEOUT);
+}
+
+template <int ELEM>
+int launch_gram_wide(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
+                     const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
+                     const int64_t* work_off, int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls,
+                     int32_t* out, cudaStream_t s) {
+    static bool configured = false;
+    if (!configured) {
+        ETM_CUDA(cudaFuncSetAttribute(gram_wide_kernel<ELEM>, cudaFuncAttributeMaxDynamicSharedMemorySize, WD_SMEM));
+        configured = true;
+    }
+    const int64_t sms = max(1, sm_count());
+    const int grid = (int)max64(1, min64(sms, n_tiles > 0 ? n_tiles : sms));
+    gram_wide_kernel<ELEM><<<grid, WD_THREADS, WD_SMEM, s>>>(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups,
+                                                             work_off, n_work, chunk_base, cls, out);
+    ETM_LAUNCHED("gram_tc");
+    return ETM_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
 // CTA-pair form (cta_group::2). A cluster of two CTAs on two SMs computes a 256 x 256 block pair
 // with one M = 256, N = 256 MMA per K step: CTA r holds A rows 128 r .. 128 r + 127 and B rows
 // 128 r .. 128 r + 127 of the blocks, the leader (rank 0) issues the MMAs and each CTA's tensor
@@ -843,11 +1074,14 @@ int gram_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, c
     // (tcgen05.st) instead of shared memory; + ETM_TC_PAIR: the CTA-pair kernel (cta_group::2).
     const bool a_tmem = (elem & ETM_TC_A_TMEM) != 0;
     const bool pair = (elem & ETM_TC_PAIR) != 0;
-    const int e = elem & ~(ETM_TC_A_TMEM | ETM_TC_PAIR);
+    const bool wide = (elem & ETM_TC_WIDE) != 0;
+    const int e = elem & ~(ETM_TC_A_TMEM | ETM_TC_PAIR | ETM_TC_WIDE);
     ETM_REQUIRE(e == 1 || e == 2, ETM_EINVAL, "gram_tc: element code %d (1 = e4m3, 2 = f16)", e);
     ETM_REQUIRE(!(pair && a_tmem), ETM_EINVAL, "gram_tc: the CTA-pair form stages both operands in shared memory");
 #define ETM_GRAM_ARGS cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, n_tiles, chunk_base, cls, out, s
+    ETM_REQUIRE(!(wide && (pair || a_tmem)), ETM_EINVAL, "gram_tc: ETM_TC_WIDE combines with no other flag");
     if (pair) return e == 2 ? launch_gram_pair<2>(ETM_GRAM_ARGS) : launch_gram_pair<1>(ETM_GRAM_ARGS);
+    if (wide) return e == 2 ? launch_gram_wide<2>(ETM_GRAM_ARGS) : launch_gram_wide<1>(ETM_GRAM_ARGS);
     if (e == 2) return a_tmem ? launch_gram<2, true>(ETM_GRAM_ARGS) : launch_gram<2, false>(ETM_GRAM_ARGS);
     return a_tmem ? launch_gram<1, true>(ETM_GRAM_ARGS) : launch_gram<1, false>(ETM_GRAM_ARGS);
 #undef ETM_GRAM_ARGS

@@ -82,14 +82,17 @@ def proj_stride(pcnt: np.ndarray, n_words: int) -> np.ndarray:
 
 
 TC_PAIR = 8  # ETM_TC_PAIR: the CTA-pair Gram kernel (tc_elem flag)
+TC_WIDE = 16  # ETM_TC_WIDE: the 256 x 256 single-CTA Gram kernel (tc_elem flag)
+#: e4m3 operands on the wide kernel: the fastest exact form measured on GB300.
+DEFAULT_TC_ELEM = 1 | TC_WIDE
 
 
-def _tile_items(m: np.ndarray, method: int, tc_elem: int = 1) -> np.ndarray:
+def _tile_items(m: np.ndarray, method: int, tc_elem: int = DEFAULT_TC_ELEM) -> np.ndarray:
     """Work items of groups of m members: 64 x 64 tile-pairs (popcount), 128 x 256 Gram items (tensor)
     or 256 x 256 block pairs (tensor, CTA-pair kernel)."""
     if method == 1:
         nb = (m + TC_TILE - 1) // TC_TILE
-        return nb * (nb + 1) // 2 if tc_elem & TC_PAIR else nb * (nb + 1)
+        return nb * (nb + 1) // 2 if tc_elem & (TC_PAIR | TC_WIDE) else nb * (nb + 1)
     nt = (m + TILE - 1) // TILE
     return nt * (nt + 1) // 2
 
@@ -219,7 +222,7 @@ class Engine:
     def __init__(self, device: torch.device | int | None = None, *, method: str = DEFAULT_METHOD,
                  form: str = "batched", chunk_cands: int = CHUNK_CANDS, small_group: int = SMALL_GROUP,
                  project: bool = True, proj_density: float = PROJ_DENSITY, proj_bytes: int = PROJ_BYTES,
-                 tc_elem: int = 1, pipeline: bool = True, autotune: "Autotuner | bool | None" = None):
+                 tc_elem: int = DEFAULT_TC_ELEM, pipeline: bool = True, autotune: "Autotuner | bool | None" = None):
         if not torch.cuda.is_available():
             raise RuntimeError("the GB300 engine needs a CUDA device; there is no CPU fallback")
         self.lib = load_library()

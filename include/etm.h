@@ -58,6 +58,10 @@ extern "C" {
  * tcgen05 cta_group::2); its work offsets count C(nb + 1, 2) block pairs per group (nb = ceil(m/256))
  * instead of nb (nb + 1) half tiles. */
 #define ETM_TC_PAIR 8
+/* Flag added to etm_count_tiles_tc's elem: the wide single-CTA kernel (one CTA per 256 x 256 block pair,
+ * two M = 128 accumulators sharing each B tile); work offsets count C(nb + 1, 2) block pairs as for
+ * ETM_TC_PAIR. */
+#define ETM_TC_WIDE 16
 
 /* Rows of one projection segment: 1024 bitvector words (65,536 transactions). */
 #define ETM_PROJ_SEG_WORDS 1024

@@ -36,8 +36,8 @@ def _k2(pkg, bv_np, method, elem=2):
     return new.rows.cpu().numpy(), new.counts.cpu().numpy()
 
 
-# 4: A operand staged in tensor memory; 8: the CTA-pair (cta_group::2) kernel
-@pytest.mark.parametrize("elem", [2, 1, 2 | 4, 1 | 4, 1 | 8, 2 | 8])
+# 4: A operand staged in tensor memory; 8: the CTA-pair (cta_group::2) kernel; 16: the 256 x 256 kernel
+@pytest.mark.parametrize("elem", [2, 1, 2 | 4, 1 | 4, 1 | 8, 2 | 8, 1 | 16, 2 | 16])
 @pytest.mark.parametrize("n_f,n_words", [(2, 1), (127, 31), (128, 32), (129, 33), (255, 4), (256, 5), (257, 3),
                                          (300, 65), (513, 6)])
 def test_pair_counts_match_popcount(pkg, n_f, n_words, elem):
@@ -50,7 +50,7 @@ def test_pair_counts_match_popcount(pkg, n_f, n_words, elem):
     assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("elem", [2, 1, 1 | 8])
+@pytest.mark.parametrize("elem", [2, 1, 1 | 8, 1 | 16, 2 | 16])
 def test_counts_exact_up_to_2_24_rows(pkg, elem):
     """All-ones columns over 2^24 - 64 rows: every pair count equals the row count exactly."""
     n_rows = (1 << 24) - 64
@@ -65,7 +65,7 @@ def test_counts_exact_up_to_2_24_rows(pkg, elem):
     assert np.array_equal(counts, want)
 
 
-@pytest.mark.parametrize("elem", [2, 1, 1 | 8])
+@pytest.mark.parametrize("elem", [2, 1, 1 | 8, 1 | 16, 2 | 16])
 @pytest.mark.parametrize("name", ["implication_plain", "implication_infer", "implication_prune", "plain_small_plain",
                                   "dense_k2_small", "deep_sparse_small", "word_tail_2049", "word_tail_65"])
 def test_tensor_engine_matches_golden(pkg, golden_cases, name, elem):
