@@ -47,6 +47,15 @@ WORKLOADS = {
 }
 
 
+#: DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic byte of a kernel, from one ncu
+#: capture of every launch of the 1M x 2048 dense K=2 workload (ncu --metrics dram__bytes_read.sum,
+#: dram__bytes_write.sum,gpu__time_duration.sum --clock-control none -k "regex:gram_wide_kernel|project_seg_kernel"
+#: python bench.py --workload dense_k2_mid --steps 1 --warmup 1 --no-plain --no-cpu --proj-gb 1: per mine
+#: 33.22 GB against 12.66 GB for the Gram, 50.51 GB against 170.35 GB for the projection); the roofline's
+#: ``traffic`` scales it to the bench's own launches by their algorithmic bytes.
+DRAM_PER_ALGORITHMIC_BYTE = {"gram_tc": 33.22 / 12.66, "project": 50.51 / 170.35}
+
+
 def _peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -125,7 +134,22 @@ LEVEL_CANDIDATES = {
 }
 
 
-def cpu_estimate(spec, level_cands, budget_s: float = 12.0, bv_host=None) -> dict:
+_MP_BV = None
+
+
+def _mp_init(bv) -> None:
+    global _MP_BV
+    _MP_BV = bv
+
+
+def _mp_count(sets) -> int:
+    from oracle import miner
+
+    miner.count_itemsets(sets, _MP_BV)
+    return len(sets)
+
+
+def cpu_estimate(spec, level_cands, budget_s: float = 12.0, bv_host=None, workers: int = 1) -> dict:
     """Seconds the CPU oracle's counting would take on the whole workload, from a timed sample.
 
     The oracle counts a candidate by ANDing its k column bitvectors and
@@ -134,6 +158,8 @@ def cpu_estimate(spec, level_cands, budget_s: float = 12.0, bv_host=None) -> dic
     a sample of candidates over full-length columns (the workload's own when
     ``bv_host`` is given, else random words of the same length) is timed and
     scaled by the level's candidate count; K=1 is one popcount per column.
+    With ``workers`` > 1 the sample is split over that many spawned processes
+    and the wall time of the whole sample is what is scaled.
     """
     from oracle import miner
 
@@ -145,6 +171,23 @@ def cpu_estimate(spec, level_cands, budget_s: float = 12.0, bv_host=None) -> dic
     else:
         n_s = min(128, bv_host.shape[0])
         bv = np.ascontiguousarray(bv_host[:n_s])
+    pool = None
+    if workers > 1:
+        import multiprocessing as mp
+
+        pool = mp.get_context("spawn").Pool(workers, initializer=_mp_init, initargs=(bv,))
+        pool.map(_mp_count, [np.zeros((1, 2), np.int32)] * workers, chunksize=1)  # workers up and importing done
+
+    def timed(sets: np.ndarray) -> float:
+        if pool is None:
+            t0 = time.perf_counter()
+            miner.count_itemsets(sets, bv)
+            return time.perf_counter() - t0
+        parts = np.array_split(sets, workers)
+        t0 = time.perf_counter()
+        pool.map(_mp_count, parts, chunksize=1)
+        return time.perf_counter() - t0
+
     per_level = []
     total = 0.0
     t_k1 = time.perf_counter()
@@ -152,23 +195,28 @@ def cpu_estimate(spec, level_cands, budget_s: float = 12.0, bv_host=None) -> dic
     t_k1 = (time.perf_counter() - t_k1) / n_s
     total += t_k1 * level_cands[0]
     per_level.append({"k": 1, "candidates": level_cands[0], "s_per_candidate": t_k1})
-    for k, n_c in enumerate(level_cands[1:], start=2):
-        sample = 256
-        while True:
-            sets = np.sort(np.stack([rng.choice(n_s, size=k, replace=False) for _ in range(sample)]), axis=1)
-            t0 = time.perf_counter()
-            miner.count_itemsets(sets.astype(np.int32), bv)
-            dt = time.perf_counter() - t0
-            if dt > budget_s / (2 * len(level_cands)) or sample >= 65536:
-                break
-            sample *= 4
-        per = dt / sample
-        total += per * n_c
-        per_level.append({"k": k, "candidates": n_c, "s_per_candidate": per, "sampled": sample})
-    return {"value": total, "unit": "s", "cores": 1, "kind": "port",
+    cap = 65536 * max(1, workers)
+    try:
+        for k, n_c in enumerate(level_cands[1:], start=2):
+            sample = 256
+            while True:
+                sets = np.sort(np.stack([rng.choice(n_s, size=k, replace=False) for _ in range(sample)]), axis=1)
+                dt = timed(sets.astype(np.int32))
+                if dt > budget_s / (2 * len(level_cands)) or sample >= cap:
+                    break
+                sample *= 4
+            per = dt / sample
+            total += per * n_c
+            per_level.append({"k": k, "candidates": n_c, "s_per_candidate": per, "sampled": sample})
+    finally:
+        if pool is not None:
+            pool.close()
+            pool.join()
+    return {"value": total, "unit": "s", "cores": max(1, workers), "kind": "port",
             "sample": "oracle/miner.py count_itemsets (AND + popcount per candidate, core/cpu_miner.py:794-809) "
-                      f"timed on sampled candidates over {n_words:,}-word columns, scaled by each level's "
-                      "candidate count",
+                      f"timed on sampled candidates over {n_words:,}-word columns"
+                      + (f", split over {workers} processes," if workers > 1 else ",")
+                      + " scaled by each level's candidate count",
             "levels": per_level}
 
 
@@ -177,7 +225,8 @@ def run_reference(args, spec) -> None:
     if cands is None:
         print(json.dumps({"impl": "reference", "unavailable": f"no recorded candidate counts for {args.workload}"}))
         return
-    base = cpu_estimate(spec, cands, budget_s=max(6.0, 30.0 / max(1, args.steps + args.warmup)))
+    base = cpu_estimate(spec, cands, budget_s=max(6.0, 30.0 / max(1, args.steps + args.warmup)),
+                        workers=max(1, os.cpu_count() or 1))
     line = {
         "impl": "reference", "metric": METRIC, "value": base["value"], "unit": "s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["value"] * 1e3, "higher_is_better": False,
@@ -406,7 +455,13 @@ def main() -> None:
             achieved = top["bytes"] / top["launches"] / per_launch_s / 1e9
             roof = {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": peaks["hbm_gbs"],
                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"]}
-        roof.update({"traffic": None, "launches_per_step": top["launches"] / args.steps,
+        ratio = DRAM_PER_ALGORITHMIC_BYTE.get(top["name"])
+        traffic = ratio * top["bytes"] / top["launches"] if ratio is not None else None
+        roof.update({"traffic": traffic, "traffic_unit": "bytes per launch",
+                     "traffic_source": "ncu DRAM bytes per algorithmic byte on the 1M x 2048 workload, scaled"
+                                       " by this run's algorithmic bytes per launch" if traffic else None,
+                     "algorithmic_bytes_per_launch": top["bytes"] / top["launches"],
+                     "launches_per_step": top["launches"] / args.steps,
                      "ms_per_step": top["ms"] / args.steps, "share_of_step": (top["ms"] / args.steps) / ms})
 
     cpu = None
@@ -415,7 +470,8 @@ def main() -> None:
     if recorded is not None:
         assert level_cands == recorded, (level_cands, recorded)
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_estimate(spec, level_cands, bv_host=bv[:128].view(torch.int64).cpu().numpy().view(np.uint64))
+        cpu = cpu_estimate(spec, level_cands, bv_host=bv[:128].view(torch.int64).cpu().numpy().view(np.uint64),
+                           workers=max(1, os.cpu_count() or 1))
 
     if rank == 0:
         line = {
