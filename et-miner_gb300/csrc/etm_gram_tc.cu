@@ -3,26 +3,32 @@
 // For a group whose members are bit rows x_0..x_{m-1} (projected suffix
 // words, or for K=2 the frequent columns themselves), the pair counts are
 // C[i][j] = popcount(x_i & x_j) = sum_r x_i[r] * x_j[r]: the Gram matrix X X^T
-// of a 0/1 matrix. One CTA per SM walks tile-pairs (ti <= tj) of 128 x 128
-// members:
+// of a 0/1 matrix. Three kernels compute it, all persistent (one CTA per SM)
+// and all with the same pipeline:
 //
-//   warps 0-7  producers: per stage (K = 64 transactions for f16, 128 for
-//              e4m3) thread t expands row t % 128 of A (t < 128) or of B: its
-//              words (prefetched a batch of 4 stages ahead into registers) become
-//              0 / s elements in the 128-byte swizzled K-major shared-memory
-//              layout the MMA reads (SWIZZLE_128B), then fence.proxy.async and
-//              an mbarrier arrive. Two producer warps per scheduler hide the
-//              latency of the expansion chains. (Variant A_TMEM: A rows go from
-//              registers straight into tensor memory with tcgen05.st, row i in
-//              TMEM lane i, halving the shared-memory traffic; exact too, but
-//              slower on GB300 because each stage waits for its TMEM stores.)
-//   warp 8     one thread issues tcgen05.mma (M=128, N=128; B from shared
-//              memory, A from shared memory or TMEM) per 16/32-element K step
-//              into a TMEM f32 accumulator, and tcgen05.commit frees each stage
+//   producers  one thread per operand row: per stage (K = 64 transactions for
+//              f16, 128 for e4m3) it expands its row's words (prefetched a
+//              batch of 4 stages ahead into registers) into elements in the
+//              128-byte swizzled K-major shared-memory layout the MMA reads
+//              (SWIZZLE_128B), then fence.proxy.async and an mbarrier arrive.
+//   MMA        one thread issues tcgen05.mma per 32-byte K step into f32
+//              accumulators in tensor memory; tcgen05.commit frees each stage
 //              and finally signals the epilogue.
-//   warps 0-7  epilogue: tcgen05.ld of their TMEM lanes (warp % 4) and column
-//              half (warp / 4), f32 -> int32, the i < j pair counts written at
-//              their lexicographic slots.
+//   epilogue   the producer warps read their TMEM lanes back with tcgen05.ld
+//              and write the i < j counts at their lexicographic slots.
+//
+//   gram_tc_kernel    128 x 256 items (A: 128 members, B: 256), 12 producer
+//                     warps, 4 stages; optionally A from tensor memory
+//                     (tcgen05.st; exact but slower on GB300).
+//   gram_wide_kernel  256 x 256 block pairs, 16 producer warps, 3 stages of
+//                     64 KB, two M = 128 MMAs per K step sharing the B tile
+//                     (accumulators in TMEM columns 0-255 and 256-511): a
+//                     third fewer shared-memory stores per unit of work. The
+//                     engine's default.
+//   gram_pair_kernel  256 x 256 block pairs over a cluster of two CTAs
+//                     (cta_group::2, M = 256); see its own comment.
+//
+// On a diagonal item the A rows are rows of B and are read from B's tile.
 //
 // Exactness: a set bit is stored as the format's smallest subnormal s
 // (f16 2^-24, e4m3 2^-9), so every product is 0 or s^2 and every partial sum
