@@ -434,7 +434,10 @@ def main() -> None:
         if i > 0:
             e2e_ms.append(dt)
         n_items_out = len(df)
-    d2h = sum(int(np.prod(lv.rows.shape)) * 4 + lv.n * 4 for lv in out.levels) + len(out.level1_cols) * 12
+    # The result comes back as item ids (int64 per item), offsets (int64) and supports (float64) per itemset.
+    n_sets = len(out.level1_cols) + sum(lv.n for lv in out.levels if lv.n)
+    n_vals = len(out.level1_cols) + sum(lv.n * lv.k for lv in out.levels if lv.n)
+    d2h = (8 * n_vals + 16 * n_sets + 8) if any(lv.n for lv in out.levels) else 0
     h2d = int(host.numel() * 8)
 
     peaks = _peaks()

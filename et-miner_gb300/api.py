@@ -340,8 +340,14 @@ def _array_facts(bv) -> tuple[tuple[int, ...], str, bool]:
 
 
 def _emit(out: MineOutput, col_items: np.ndarray):
-    levels = [(col_items[cols], counts) for cols, counts in out.host_levels()]
-    return _frame(levels, out.n_rows, col_items.dtype == np.uint64)
+    """The result frame; item ids, offsets and supports are built on the device (``frame_arrays``)."""
+    offsets, values, support, _ = out.frame_arrays(col_items)
+    frame = ItemsetFrame(offsets, values, support)
+    if _pl is not None:
+        return frame.to_polars()
+    if pa is not None:
+        return frame.to_arrow()
+    return frame
 
 
 def _session_from(out: MineOutput, session: ProfilingSession) -> None:

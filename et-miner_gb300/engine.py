@@ -167,6 +167,46 @@ class MineOutput:
     def n_itemsets(self) -> int:
         return len(self.level1_cols) + sum(lv.n for lv in self.levels)
 
+    def frame_arrays(self, item_of_col: np.ndarray) -> tuple[np.ndarray, np.ndarray, np.ndarray, int]:
+        """The result as flat arrays, built on the device and copied back once: (offsets int64 [n + 1],
+        item ids [offsets[-1]] (int64, or uint64 when ``item_of_col`` is), support float64 [n]) for
+        every emitted itemset in level order, and the bytes copied device to host.
+
+        ``item_of_col[c]`` is the item id of the caller's column c.
+        """
+        wide = item_of_col.dtype == np.uint64
+
+        def as_i64(a: np.ndarray) -> np.ndarray:
+            a = np.ascontiguousarray(a)
+            return a.view(np.int64) if wide else a.astype(np.int64)
+
+        n1 = len(self.level1_cols)
+        lv_on = [lv for lv in self.levels if lv.n > 0]
+        if not lv_on:
+            values = as_i64(item_of_col[self.level1_cols])
+            offsets = np.arange(n1 + 1, dtype=np.int64)
+            support = self.level1_counts.astype(np.float64) / max(1, self.n_rows)
+            return offsets, values.view(np.uint64) if wide else values, support, 0
+        dev = lv_on[0].rows.device
+        table = torch.from_numpy(as_i64(item_of_col[self.gen_cols])).to(dev)
+        vparts = [torch.from_numpy(as_i64(item_of_col[self.level1_cols])).to(dev)]
+        cparts = [torch.from_numpy(self.level1_counts.astype(np.int64)).to(dev)]
+        oparts = [torch.arange(0, n1 + 1, dtype=torch.int64, device=dev)]
+        base = n1
+        for lv in lv_on:
+            vparts.append(table[lv.rows.reshape(-1).long()])
+            cparts.append(lv.counts.to(torch.int64))
+            oparts.append(base + lv.k * torch.arange(1, lv.n + 1, dtype=torch.int64, device=dev))
+            base += lv.k * lv.n
+        values_d = torch.cat(vparts)
+        support_d = torch.cat(cparts).to(torch.float64) / max(1, self.n_rows)
+        offsets_d = torch.cat(oparts)
+        values = values_d.cpu().numpy()
+        support = support_d.cpu().numpy()
+        offsets = offsets_d.cpu().numpy()
+        d2h = values.nbytes + support.nbytes + offsets.nbytes
+        return offsets, values.view(np.uint64) if wide else values, support, d2h
+
 
 class _Scratch:
     """Reusable device buffers, grown on demand (torch allocations: plumbing only)."""
