@@ -220,6 +220,18 @@ def cpu_estimate(spec, level_cands, budget_s: float = 12.0, bv_host=None, worker
             "levels": per_level}
 
 
+def max_over_ranks(value: float, dist=None, device: str = "cuda") -> float:
+    """The largest of every rank's ``value`` (the replicas' slowest mine); ``value`` itself without a process
+    group."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args, spec) -> None:
     cands = LEVEL_CANDIDATES.get(args.workload)
     if cands is None:
@@ -397,10 +409,7 @@ def main() -> None:
     clk = clocks.stop()
     ms = start.elapsed_time(end) / args.steps
     launches = (eng.launches - launches0) // args.steps
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist, "cuda")
     kern = eng.kernel_report()
 
     # Plain form (one counting launch per prefix group): the comparator.

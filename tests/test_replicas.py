@@ -1,0 +1,70 @@
+"""The replicas path of bench.py on CPU: two gloo ranks agree on the slowest rank's time, and the
+reference arm runs on rank 0 only."""
+
+from __future__ import annotations
+
+import os
+import socket
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank: int, world: int, port: int, q) -> None:
+    import torch.distributed as dist
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        v = bench.max_over_ranks(1.5 + rank, dist, "cpu")
+        dist.barrier()
+        q.put((rank, v))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_max_over_ranks_with_two_gloo_ranks():
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    try:
+        got = sorted(q.get(timeout=120) for _ in range(2))
+    finally:
+        for p in procs:
+            p.join(timeout=60)
+    assert got == [(0, 2.5), (1, 2.5)]
+    assert all(p.exitcode == 0 for p in procs)
+
+
+def test_max_over_ranks_without_process_group():
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    assert bench.max_over_ranks(3.25) == 3.25
+
+
+@pytest.mark.parametrize("rank", ["1"])
+def test_reference_arm_prints_nothing_on_other_ranks(rank):
+    env = dict(os.environ, RANK=rank, WORLD_SIZE="2", LOCAL_RANK=rank)
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--gpus", "2"],
+                       capture_output=True, text=True, env=env, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip() == ""
