@@ -469,7 +469,7 @@ template <int ELEM, bool A_TMEM>
 int launch_gram(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                 const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
                 int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t* out,
-                cudaStream_t s) {
+                int64_t* /*work_counter: items go round-robin*/, cudaStream_t s) {
     static bool configured = false;
     if (!configured) {
         ETM_CUDA(cudaFuncSetAttribute(gram_tc_kernel<ELEM, A_TMEM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -503,7 +503,8 @@ __global__ void __launch_bounds__(WD_THREADS, 1) gram_wide_kernel(
     const uint64_t* __restrict__ src, const int64_t* __restrict__ cbase, const int64_t* __restrict__ cwords,
     const int64_t* __restrict__ cld, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
     const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
-    const uint8_t* __restrict__ cls, int32_t* __restrict__ out) {
+    const uint8_t* __restrict__ cls, int32_t* __restrict__ out,
+    unsigned long long* __restrict__ work_counter) {
     constexpr int WORDS_PER_STAGE = ELEM == 2 ? 1 : 2;
     extern __shared__ uint8_t dsmem[];
     __shared__ __align__(8) uint64_t full_bar[WD_STAGES];
@@ -514,6 +515,7 @@ __global__ void __launch_bounds__(WD_THREADS, 1) gram_wide_kernel(
     __shared__ int abort_sh;
     __shared__ int64_t off_a[WD_TILE];
     __shared__ int64_t off_b[WD_TILE];
+    __shared__ int64_t next_sh;
 
     uint8_t* slots = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x;
@@ -544,7 +546,16 @@ __global__ void __launch_bounds__(WD_THREADS, 1) gram_wide_kernel(
     const int64_t total = work_off[n_work];
     int64_t gstage = 0;
     uint32_t tile_iter = 0;
-    for (int64_t tp = blockIdx.x; tp < total; tp += gridDim.x) {
+    // Block pairs in work-list order; with a work counter each CTA takes the next unclaimed one
+    // (dynamic balance across groups of different lengths), else every gridDim.x-th.
+    auto next_item = [&](int64_t tp) -> int64_t {
+        if (tid == 0)
+            next_sh = work_counter != nullptr ? (int64_t)gridDim.x + (int64_t)atomicAdd(work_counter, 1ULL)
+                                               : tp + gridDim.x;
+        __syncthreads();
+        return next_sh;
+    };
+    for (int64_t tp = blockIdx.x; tp < total; tp = next_item(tp)) {
         const int64_t wi = upper_find(work_off, n_work, tp);
         const int64_t g = work_groups[wi];
         const int64_t m = grp_size[g];
@@ -701,7 +712,7 @@ template <int ELEM>
 int launch_gram_wide(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                      const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
                      const int64_t* work_off, int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls,
-                     int32_t* out, cudaStream_t s) {
+                     int32_t* out, int64_t* work_counter, cudaStream_t s) {
     static bool configured = false;
     if (!configured) {
         ETM_CUDA(cudaFuncSetAttribute(gram_wide_kernel<ELEM>, cudaFuncAttributeMaxDynamicSharedMemorySize, WD_SMEM));
@@ -709,8 +720,10 @@ int launch_gram_wide(const uint64_t* cbuf, const int64_t* cbase, const int64_t* 
     }
     const int64_t sms = max(1, sm_count());
     const int grid = (int)max64(1, min64(sms, n_tiles > 0 ? n_tiles : sms));
+    if (work_counter != nullptr) ETM_CUDA(cudaMemsetAsync(work_counter, 0, sizeof(int64_t), s));
     gram_wide_kernel<ELEM><<<grid, WD_THREADS, WD_SMEM, s>>>(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups,
-                                                             work_off, n_work, chunk_base, cls, out);
+                                                             work_off, n_work, chunk_base, cls, out,
+                                                             reinterpret_cast<unsigned long long*>(work_counter));
     ETM_LAUNCHED("gram_tc");
     return ETM_OK;
 }
@@ -1040,7 +1053,7 @@ template <int ELEM>
 int launch_gram_pair(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                      const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
                      const int64_t* work_off, int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls,
-                     int32_t* out, cudaStream_t s) {
+                     int32_t* out, int64_t* /*work_counter: items go round-robin*/, cudaStream_t s) {
     static bool configured = false;
     static int max_clusters = 0;
     if (!configured) {
@@ -1075,7 +1088,7 @@ namespace etm {
 int gram_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
             const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
             int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t elem, int32_t* out,
-            cudaStream_t s) {
+            int64_t* work_counter, cudaStream_t s) {
     // elem: 1 = e4m3, 2 = f16; + ETM_TC_A_TMEM: the A operand is staged in tensor memory
     // (tcgen05.st) instead of shared memory; + ETM_TC_PAIR: the CTA-pair kernel (cta_group::2).
     const bool a_tmem = (elem & ETM_TC_A_TMEM) != 0;
@@ -1084,7 +1097,7 @@ int gram_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, c
     const int e = elem & ~(ETM_TC_A_TMEM | ETM_TC_PAIR | ETM_TC_WIDE);
     ETM_REQUIRE(e == 1 || e == 2, ETM_EINVAL, "gram_tc: element code %d (1 = e4m3, 2 = f16)", e);
     ETM_REQUIRE(!(pair && a_tmem), ETM_EINVAL, "gram_tc: the CTA-pair form stages both operands in shared memory");
-#define ETM_GRAM_ARGS cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, n_tiles, chunk_base, cls, out, s
+#define ETM_GRAM_ARGS cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, n_tiles, chunk_base, cls, out, work_counter, s
     ETM_REQUIRE(!(wide && (pair || a_tmem)), ETM_EINVAL, "gram_tc: ETM_TC_WIDE combines with no other flag");
     if (pair) return e == 2 ? launch_gram_pair<2>(ETM_GRAM_ARGS) : launch_gram_pair<1>(ETM_GRAM_ARGS);
     if (wide) return e == 2 ? launch_gram_wide<2>(ETM_GRAM_ARGS) : launch_gram_wide<1>(ETM_GRAM_ARGS);
@@ -1106,11 +1119,11 @@ extern "C" int etm_count_tiles_tc(const uint64_t* cbuf, const int64_t* cbase, co
                                   const int64_t* cld, const int32_t* grp_size, const int64_t* cand_off,
                                   const int64_t* work_groups, const int64_t* work_off, int64_t n_work,
                                   int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t elem,
-                                  int32_t* out_counts, void* stream) {
+                                  int32_t* out_counts, int64_t* work_counter, void* stream) {
     ETM_REQUIRE((reinterpret_cast<uintptr_t>(cbuf) & 15) == 0, ETM_EINVAL, "etm_count_tiles_tc: cbuf must be 16-byte aligned");
     if (n_work <= 0) return ETM_OK;
     return etm::gram_tc(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, n_tiles,
-                        chunk_base, cls, elem, out_counts, as_stream(stream));
+                        chunk_base, cls, elem, out_counts, work_counter, as_stream(stream));
 }
 
 extern "C" int etm_device_status(void* stream) {

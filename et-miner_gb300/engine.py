@@ -389,6 +389,8 @@ class Engine:
         projection of the next chunk can run while the current one is counted.
         """
         width = gen.k
+        # Longest prefixes first: the Gram's CTAs claim block pairs in this order, so the last ones are short.
+        gids = gids[np.argsort(-pcnt[gids], kind="stable")]
         m = sizes[gids]
         cnt = pcnt[gids]
         n_seg = max(1, -(-n_words // PROJ_SEG_WORDS))
@@ -442,9 +444,12 @@ class Engine:
         ``macs`` is the useful work: one multiply-add per candidate pair and row (sum of C(m,2) x rows).
         """
         if method == 1:
+            # The work counter lets the Gram's CTAs claim block pairs dynamically (one per engine: the Gram
+            # launches of an engine run in turn on its main stream).
+            counter = self.scratch.get("tc_work_counter", 1, torch.int64)
             st = self._launch("gram_tc", nbytes, lambda: self.lib.etm_count_tiles_tc(
                 _p(cbuf), _p(cbase), _p(cwords), _p(cld), _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, n_tiles,
-                base, _p(cls), self.tc_elem, _p(counts), _stream()), flops=2 * macs)
+                base, _p(cls), self.tc_elem, _p(counts), _p(counter), _stream()), flops=2 * macs)
             check(st, "etm_count_tiles_tc")
             self.used_tensor = True
         else:

@@ -242,14 +242,18 @@ int etm_count_tiles_proj(const uint64_t* cbuf, const int64_t* cbase, const int64
  * accumulation in TMEM. Exact while every group has at most 2^24 rows
  * (cwords <= 262144): the caller sends larger groups to the popcount kernels.
  * work_off counts work items: nb(nb+1) per group, nb = ceil(m/256) (the two
- * 128-member halves of super-tile ua against super-tile ub, ua <= ub);
- * n_tiles = work_off[n_work] (sizes the grid). New in this engine (the
- * reference counts on CUDA cores only).
+ * 128-member halves of super-tile ua against super-tile ub, ua <= ub; with
+ * ETM_TC_WIDE or ETM_TC_PAIR the C(nb + 1, 2) block pairs ua <= ub);
+ * n_tiles = work_off[n_work] (sizes the grid). work_counter (one int64 of
+ * device memory, or NULL) lets the ETM_TC_WIDE kernel's CTAs claim items
+ * dynamically (it is zeroed on the stream before the launch; concurrent calls
+ * need separate counters); the other kernels take items round-robin. New in
+ * this engine (the reference counts on CUDA cores only).
  */
 int etm_count_tiles_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                        const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
                        const int64_t* work_off, int64_t n_work, int64_t n_tiles, int64_t chunk_base,
-                       const uint8_t* cls, int32_t elem, int32_t* out_counts, void* stream);
+                       const uint8_t* cls, int32_t elem, int32_t* out_counts, int64_t* work_counter, void* stream);
 
 /*
  * Reads and clears the device status word the tensor-core kernels raise when a
