@@ -290,7 +290,8 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
                                                          int64_t n_seg, const int64_t* __restrict__ seg_off,
                                                          const int64_t* __restrict__ cbase,
                                                          const int64_t* __restrict__ cld,
-                                                         uint64_t* __restrict__ cbuf) {
+                                                         uint64_t* __restrict__ cbuf,
+                                                         unsigned long long* __restrict__ work_counter) {
     extern __shared__ __align__(16) uint8_t psmem[];
     uint64_t* stage = reinterpret_cast<uint64_t*>(psmem);  // NSTAGE x (SEG_W member words + zero pad)
     uint64_t* pw = reinterpret_cast<uint64_t*>(psmem + NSTAGE * STAGE_BYTES);  // SEG_W prefix words
@@ -298,11 +299,20 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
     __shared__ int32_t pref[64];
     __shared__ uint64_t park[P_WARPS * MPI * 4 * MAX_CHUNKS];
     __shared__ int32_t ids[ID_RING];
+    __shared__ int64_t next_sh;
     const int plen = width - 1;
     const int64_t total = n_seg * n_work;
     if (threadIdx.x < 2 * NSTAGE)  // the zero pads after the stage buffers (cp.async never writes them)
         reinterpret_cast<uint64_t*>(psmem + (threadIdx.x >> 1) * STAGE_BYTES + SEG_W * 8)[threadIdx.x & 1] = 0ULL;
-    for (int64_t q = blockIdx.x; q < total; q += gridDim.x) {
+    // Units in segment-major order; with a work counter each CTA claims the next unclaimed one.
+    auto next_unit = [&](int64_t q) -> int64_t {
+        if (threadIdx.x == 0)
+            next_sh = work_counter != nullptr ? (int64_t)gridDim.x + (int64_t)atomicAdd(work_counter, 1ULL)
+                                               : q + gridDim.x;
+        __syncthreads();
+        return next_sh;
+    };
+    for (int64_t q = blockIdx.x; q < total; q = next_unit(q)) {
         const int64_t s = q / n_work, wi = q - s * n_work;
         const int64_t g = work_groups[wi];
         const int64_t m = grp_size[g];
@@ -418,7 +428,7 @@ extern "C" int etm_prefix_segments(const uint64_t* fbv, int64_t ld, int64_t n_wo
 extern "C" int etm_project(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
                            const int64_t* grp_first, const int32_t* grp_size, const int64_t* work_groups,
                            int64_t n_work, const int64_t* seg_off, const int64_t* cbase, const int64_t* cld,
-                           uint64_t* cbuf, void* stream) {
+                           uint64_t* cbuf, int64_t* work_counter, void* stream) {
     ETM_REQUIRE(width >= 2 && width <= 64, ETM_EINVAL, "etm_project: width %d out of range (2..64)", width);
     ETM_REQUIRE(ld >= n_words && n_words >= 0 && ld % 2 == 0, ETM_EINVAL, "etm_project: ld must be even and >= n_words");
     ETM_REQUIRE((reinterpret_cast<uintptr_t>(fbv) & 15) == 0, ETM_EINVAL, "etm_project: fbv must be 16-byte aligned");
@@ -431,9 +441,11 @@ extern "C" int etm_project(const uint64_t* fbv, int64_t ld, int64_t n_words, con
     const int64_t n_seg = ceil_div<int64_t>(n_words, SEG_W);
     const int64_t units = n_seg * n_work;
     const int grid = (int)min64(units, (int64_t)max(1, sm_count()) * 2);
+    if (work_counter != nullptr) ETM_CUDA(cudaMemsetAsync(work_counter, 0, sizeof(int64_t), as_stream(stream)));
     project_seg_kernel<<<grid, PT, PROJ_SMEM, as_stream(stream)>>>(fbv, ld, n_words, rows, width, grp_first, grp_size,
                                                                    work_groups, n_work, n_seg, seg_off, cbase, cld,
-                                                                   cbuf);
+                                                                   cbuf,
+                                                                   reinterpret_cast<unsigned long long*>(work_counter));
     ETM_LAUNCHED("project");
     return ETM_OK;
 }

@@ -407,6 +407,7 @@ class Engine:
         wg, wo = d[:n], d[n:2 * n + 1]
         cbase, cwords, cld = d[2 * n + 1:3 * n + 1], d[3 * n + 1:4 * n + 1], d[4 * n + 1:5 * n + 1]
         seg_off = self.scratch.get(f"proj_seg_{buf}", n * (n_seg + 1), torch.int64)
+        proj_counter = self.scratch.get(f"proj_counter_{buf}", 1, torch.int64)
         cbuf = self.scratch.get(f"proj_cbuf_{buf}", int(cb[-1]), torch.int64)
         st = self._launch("prefix_segments", int(n * (width - 1) * n_words * 8),
                           lambda: self.lib.etm_prefix_segments(_p(fbv), ldp, n_words, _p(gen.rows), width,
@@ -417,7 +418,7 @@ class Engine:
         st = self._launch("project", int(((m + width - 1) * n_words).sum() * 8 + (m * cl).sum() * 8),
                           lambda: self.lib.etm_project(_p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first),
                                                        _p(grp_size), _p(wg), n, _p(seg_off), _p(cbase), _p(cld),
-                                                       _p(cbuf), _stream()))
+                                                       _p(cbuf), _p(proj_counter), _stream()))
         check(st, "etm_project")
         self.launches += 2
         return dict(d=d, cbuf=cbuf, cbase=cbase, cwords=cwords, cld=cld, wg=wg, wo=wo, n=n, n_tiles=int(toff[-1]),

@@ -214,6 +214,9 @@ int etm_triple_counts_rows(const int64_t* row_ptr, const int32_t* cols, int64_t 
  *                      (cld % 32 == 0, cbase even, ld even, fbv 16-byte aligned).
  *                      Padding rows are zero in every member, so pair counts
  *                      over the projected words equal those over the prefix rows.
+ *                      work_counter (one int64 of device memory, or NULL): the
+ *                      CTAs claim (segment, group) units from it dynamically; it
+ *                      is zeroed on the stream first (one per concurrent call).
  *   etm_count_tiles_proj  etm_count_tiles over the projected words
  *                      (cwords[wi] words per member; no prefix AND).
  */
@@ -228,7 +231,8 @@ int etm_prefix_segments(const uint64_t* fbv, int64_t ld, int64_t n_words, const 
                         int64_t* out_words, void* stream);
 int etm_project(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
                 const int64_t* grp_first, const int32_t* grp_size, const int64_t* work_groups, int64_t n_work,
-                const int64_t* seg_off, const int64_t* cbase, const int64_t* cld, uint64_t* cbuf, void* stream);
+                const int64_t* seg_off, const int64_t* cbase, const int64_t* cld, uint64_t* cbuf,
+                int64_t* work_counter, void* stream);
 int etm_count_tiles_proj(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                          const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
                          const int64_t* work_off, int64_t n_work, int64_t chunk_base, const uint8_t* cls,

@@ -352,10 +352,13 @@ def test_segmented_projection(pkg, lib, n_words, width):
                                  d_wg.data_ptr(), len(wg), seg_off.data_ptr(), out_words.data_ptr(), _stream())
     assert st == 0, lib.etm_last_error()
     cbuf = torch.full((int(cb[-1]),), -1, dtype=torch.int64, device="cuda")
+    # Alternate the dynamic (work counter) and round-robin unit orders across the cases.
+    ctr = torch.zeros(1, dtype=torch.int64, device="cuda")  # held for the call
+    counter = ctr.data_ptr() if n_words % 2 else None
     d_cbase, d_cld = _dev(cb[:-1].copy()), _dev(cl)
     st = lib.etm_project(d_fbv.data_ptr(), ld, n_words, d_rows.data_ptr(), width, d_first.data_ptr(),
                          d_size.data_ptr(), d_wg.data_ptr(), len(wg), seg_off.data_ptr(), d_cbase.data_ptr(),
-                         d_cld.data_ptr(), cbuf.data_ptr(), _stream())
+                         d_cld.data_ptr(), cbuf.data_ptr(), counter, _stream())
     assert st == 0, lib.etm_last_error()
     got = cbuf.cpu().numpy().view(np.uint64)
     want = _projection_reference(bits.astype(bool), ld, n_words, [groups[g] for g in wg], cl)
