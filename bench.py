@@ -51,9 +51,9 @@ WORKLOADS = {
 #: capture of every launch of the 1M x 2048 dense K=2 workload (ncu --metrics dram__bytes_read.sum,
 #: dram__bytes_write.sum,gpu__time_duration.sum --clock-control none -k "regex:gram_wide_kernel|project_seg_kernel"
 #: python bench.py --workload dense_k2_mid --steps 1 --warmup 1 --no-plain --no-cpu --proj-gb 1: per mine
-#: 33.22 GB against 12.66 GB for the Gram, 50.51 GB against 170.35 GB for the projection); the roofline's
+#: 16.21 GB against 12.66 GB for the Gram, 19.41 GB against 170.35 GB for the projection); the roofline's
 #: ``traffic`` scales it to the bench's own launches by their algorithmic bytes.
-DRAM_PER_ALGORITHMIC_BYTE = {"gram_tc": 33.22 / 12.66, "project": 50.51 / 170.35}
+DRAM_PER_ALGORITHMIC_BYTE = {"gram_tc": 16.21 / 12.66, "project": 19.41 / 170.35}
 
 
 def _peaks() -> dict:
