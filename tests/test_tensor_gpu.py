@@ -93,3 +93,54 @@ def test_dense_bernoulli_tensor_matches_popcount(pkg):
     assert len(a) == len(b)
     for (ra, ca), (rb, cb) in zip(a, b):
         assert np.array_equal(ra, rb) and np.array_equal(ca, cb)
+
+
+@pytest.mark.parametrize("with_counter", [True, False])
+def test_wide_kernel_claimed_and_round_robin_items_agree(pkg, with_counter):
+    """etm_count_tiles_tc with ETM_TC_WIDE over several groups of different sizes and lengths: block pairs
+    claimed from a work counter or taken round-robin give the same counts, equal to a host Gram."""
+    import torch
+
+    lib = pkg.load_library()
+    rng = np.random.default_rng(11)
+    sizes = np.array([300, 1, 2, 257, 513, 40], np.int64)
+    cw = np.array([64, 2, 3, 130, 17, 1], np.int64)  # words per member row (odd counts end in a half stage)
+    cld = (cw + 31) // 32 * 32
+    cbase = np.zeros(len(sizes), np.int64)
+    cbase[1:] = np.cumsum(sizes * cld)[:-1]
+    total_words = int((sizes * cld).sum())
+    buf = np.zeros(total_words, np.uint64)
+    want = []
+    for g in range(len(sizes)):
+        m, w = int(sizes[g]), int(cw[g])
+        x = rng.integers(0, 2**63, size=(m, w), dtype=np.int64).view(np.uint64)
+        x &= rng.integers(0, 2**63, size=(m, w), dtype=np.int64).view(np.uint64)
+        rows = buf[cbase[g]:cbase[g] + m * cld[g]].reshape(m, cld[g])
+        rows[:, :w] = x
+        bits = np.unpackbits(x.view(np.uint8), axis=1).astype(np.int64)
+        gram = bits @ bits.T
+        want.append(gram[np.triu_indices(m, 1)])
+    want = np.concatenate(want).astype(np.int32)
+    pairs = sizes * (sizes - 1) // 2
+    cand_off = np.zeros(len(sizes) + 1, np.int64)
+    np.cumsum(pairs, out=cand_off[1:])
+    nb = (sizes + 255) // 256
+    items = nb * (nb + 1) // 2
+    work_off = np.zeros(len(sizes) + 1, np.int64)
+    np.cumsum(items, out=work_off[1:])
+    d = {k: torch.from_numpy(v).cuda() for k, v in dict(
+        buf=buf.view(np.int64), cbase=cbase, cwords=cw, cld=cld, size=sizes.astype(np.int32),
+        cand_off=cand_off, wg=np.arange(len(sizes), dtype=np.int64), wo=work_off).items()}
+    out = torch.full((int(cand_off[-1]),), -7, dtype=torch.int32, device="cuda")
+    counter = torch.full((1,), 12345, dtype=torch.int64, device="cuda")  # zeroed by the call
+    st = lib.etm_count_tiles_tc(d["buf"].data_ptr(), d["cbase"].data_ptr(), d["cwords"].data_ptr(),
+                                d["cld"].data_ptr(), d["size"].data_ptr(), d["cand_off"].data_ptr(),
+                                d["wg"].data_ptr(), d["wo"].data_ptr(), len(sizes), int(work_off[-1]), 0, None,
+                                1 | 16, out.data_ptr(), counter.data_ptr() if with_counter else None,
+                                torch.cuda.current_stream().cuda_stream)
+    assert st == 0, lib.etm_last_error()
+    assert np.array_equal(out.cpu().numpy(), want)
+    if with_counter:
+        # Each CTA starts on item blockIdx.x, claims one item after each it finishes, and stops at its
+        # first claim past the end: (items - grid) claims that succeed + grid that fail = items.
+        assert int(counter.item()) == int(work_off[-1])
