@@ -688,11 +688,13 @@ class Engine:
                             _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
                             _p(wg), _p(wo), len(bg), base, _p(cls), _p(counts), _stream()))
                     else:
-                        # Each group's prefix and suffix columns, once (the same-data minimum).
+                        # Each group's prefix and suffix columns, once (the same-data minimum). Groups that reach
+                        # this kind under the tensor method hold more than 2^24 rows (past the f32-exact range
+                        # of the Gram), so these tiles always count on the CUDA cores.
                         nbytes = int((mg + width - 1).sum()) * n_words * 8
                         st = self._launch("count_tiles", nbytes, lambda: self.lib.etm_count_tiles(
                             _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
-                            _p(wg), _p(wo), len(bg), base, _p(cls), method, _p(counts), _stream()))
+                            _p(wg), _p(wo), len(bg), base, _p(cls), 0, _p(counts), _stream()))
                     check(st, f"etm_count_{kind}")
                     self.launches += 1
             if pipelined and c + 1 < len(chunks):

@@ -192,3 +192,20 @@ def test_row_wise_k3_is_used_and_exact(pkg, golden_cases):
     assert len(got.levels) == len(ref.levels)
     for a, b in zip(got.levels, ref.levels):
         assert torch.equal(a.rows, b.rows) and torch.equal(a.counts, b.counts)
+
+
+@pytest.mark.parametrize("name", ["dense_k2_small", "implication_infer", "deep_sparse_small"])
+def test_tensor_engine_past_the_exact_row_limit(pkg, golden_cases, monkeypatch, name):
+    """Groups over the Gram's exact row limit (2^24 prefix rows; lowered here to 100) and a K=2 level over more
+    rows than it count on the CUDA cores within the tensor engine, with the same results."""
+    from importlib import import_module
+
+    engm = import_module(pkg.__name__ + ".engine")
+    monkeypatch.setattr(engm, "TC_MAX_ROWS", 100)
+    case = golden_cases[name]
+    indptr, items, n_rows = case_input(pkg, case)
+    got = pkg.apriori(table_of(indptr, items, n_rows), min_support=case["min_support"], max_length=case["max_length"],
+                      use_gpu=True, prune_equal_support=case["prune_equal_support"],
+                      use_generator_pruning=case["use_generator_pruning"], engine=engm.Engine(method="tensor"),
+                      warn_complexity=False)
+    assert digest_pairs(pkg.result_pairs(got, n_rows)) == case["digest"]
