@@ -27,7 +27,7 @@ _LAZY = {
 
 
 def __getattr__(name):
-    # The driver modules import torch; load them on first use.
+    # The engine, API and serving modules import torch; load them on first use.
     mod = _LAZY.get(name)
     if mod is None:
         raise AttributeError(name)

@@ -1,6 +1,6 @@
 """CPU oracle: a numpy restatement of ET-Miner's CPU mining route (test infrastructure only).
 
-This module is the CHECKER for the GPU engine. Only ``tests/``,
+This module is the oracle the GPU engine is checked against. Only ``tests/``,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may
 import it; the engine itself never does, and never falls back to it.
 
