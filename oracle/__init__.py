@@ -1,7 +1,7 @@
 """CPU oracle for the GB300 Apriori engine: test infrastructure, never on the product path.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
-use this package. ``miner`` restates ET-Miner's CPU mining route in numpy;
-``etm_oracle.c`` restates its counting core in C (OpenMP) for the larger
-workloads and the timed CPU baseline.
+use this package. ``miner`` restates ET-Miner's CPU mining route in numpy; the
+timed CPU baseline runs its per-candidate counting over all host cores in
+spawned processes.
 """
