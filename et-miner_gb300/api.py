@@ -210,6 +210,59 @@ def _frequent_csr(indptr: np.ndarray, flat: np.ndarray, n_rows: int, mc: int):
     return row_ptr, cols, items[keep]
 
 
+def _frequent_csr_device(indptr: np.ndarray, flat: np.ndarray, n_rows: int, mc: int, device):
+    """``_frequent_csr`` on the device: (row_ptr int64 [n_rows+1] and column ids int32 as device tensors, the
+    items of the columns and the rows' lengths on the host).
+
+    The same steps as the host version (sort the ids, drop repeated (row, item) pairs, keep the items
+    with count >= mc, number them in ascending id order), with device sorts; UInt64 ids are sorted
+    through their sign-flipped int64 bits, which orders them as unsigned values.
+    """
+    import torch
+
+    sign = -(2**63)
+    wide = flat.dtype == np.uint64
+    host = np.ascontiguousarray(flat).view(np.int64) if wide else np.ascontiguousarray(flat).astype(np.int64, copy=False)
+    vals = torch.from_numpy(host).to(device)
+    if wide:
+        vals = vals ^ sign
+    lens = torch.from_numpy(np.diff(indptr).astype(np.int64)).to(device)
+    rid = torch.repeat_interleave(torch.arange(n_rows, dtype=torch.int64, device=device), lens)
+    items, inv = torch.unique(vals, sorted=True, return_inverse=True)
+    n_items = max(1, items.numel())
+    key = torch.unique(rid * n_items + inv)  # ascending: by row, then by item
+    del rid, inv, vals
+    rid, inv = key // n_items, key % n_items
+    counts = torch.bincount(inv, minlength=items.numel())
+    keep = counts >= max(1, mc)
+    remap = torch.cumsum(keep.to(torch.int64), 0) - 1
+    sel = keep[inv]
+    cols = remap[inv[sel]].to(torch.int32)
+    row_len = torch.bincount(rid[sel], minlength=n_rows)
+    row_ptr = torch.zeros(n_rows + 1, dtype=torch.int64, device=device)
+    torch.cumsum(row_len, 0, out=row_ptr[1:])
+    kept = items[keep]
+    if wide:
+        kept = kept ^ sign
+    kept_h = kept.cpu().numpy()
+    return row_ptr, cols, (kept_h.view(np.uint64) if wide else kept_h), row_len.cpu().numpy()
+
+
+def _bitvecs_of_device_csr(row_ptr, cols, n_cols: int, n_rows: int):
+    """Column bitvectors [n_cols, ceil(N/64)] (torch int64) from a device CSR (etm_build_bitvecs)."""
+    import torch
+
+    from ._lib import check, load_library
+
+    lib = load_library()
+    ld = max(1, (n_rows + 63) // 64)
+    bv = torch.empty((max(n_cols, 1), ld), dtype=torch.int64, device=row_ptr.device)
+    ids = cols if cols.numel() else torch.zeros(1, dtype=torch.int32, device=row_ptr.device)
+    check(lib.etm_build_bitvecs(row_ptr.data_ptr(), ids.data_ptr(), cols.numel(), None, 0, n_rows, n_cols, ld,
+                                bv.data_ptr(), torch.cuda.current_stream().cuda_stream), "etm_build_bitvecs")
+    return bv[:n_cols]
+
+
 def build_device_bitvecs(row_ptr: np.ndarray, cols: np.ndarray, n_cols: int, n_rows: int, device=None,
                          keep_rows: bool = False):
     """Column bitvectors [n_cols, ceil(N/64)] (torch int64 view of uint64) built on the device by etm_build_bitvecs.
@@ -457,11 +510,12 @@ def apriori(
         raise ValueError(f"n_transactions={n_rows:,} exceeds int32 max")
     wide = np.dtype(kind) == np.uint64
     mc = min_count(min_support, n_rows)
-    row_ptr, cols, items = _frequent_csr(indptr, flat, n_rows, mc)
+    row_ptr, cols, items, row_len = _frequent_csr_device(indptr, flat, n_rows, mc, eng.device)
     if len(items) == 0:
         df = _frame([], max(1, n_rows), wide)
         return (df, session) if profile else df
-    bv, rows = build_device_bitvecs(row_ptr, cols, len(items), n_rows, keep_rows=True)
+    bv = _bitvecs_of_device_csr(row_ptr, cols, len(items), n_rows)
+    rows = (row_ptr, cols, row_len)
     max_tx = int(np.diff(indptr).max()) if n_rows else 0
     eff = min(max_length, max_tx) if max_length else max_tx
     out = eng.mine(bv, n_rows, min_support, eff if eff >= 1 else 1, prune_equal_support=prune_equal_support,
