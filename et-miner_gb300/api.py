@@ -9,10 +9,10 @@ Same signature, parameter validation and error types as the reference's
   (core/apriori.py:477-548);
 * ``transactions`` with ``use_gpu=True``: a list column (polars DataFrame or
   LazyFrame when polars is installed, a pyarrow Table, a dict of lists, or a
-  plain list of item lists). The items are deduplicated per row and counted
-  on the host, the frequent ones coded to columns, and the column bitvectors
-  are built on the device by ``etm_build_bitvecs`` (the reference's input
-  layer, gpu/input_layer.py:469-544 and gpu/csr_bitvec.py:63-155).
+  plain list of item lists). On the device the items are deduplicated per
+  row and counted, the frequent ones coded to columns in ascending id order,
+  and the column bitvectors built by ``etm_build_bitvecs`` (the reference's
+  input layer, gpu/input_layer.py:469-544 and gpu/csr_bitvec.py:63-155).
 
 The routes this engine does not implement (the CPU route, SON streaming,
 several GPUs, the per-level parquet flush, resume, anchors) raise
@@ -192,7 +192,9 @@ def _python_rows(rows) -> tuple[np.ndarray, np.ndarray, np.dtype]:
 
 
 def _frequent_csr(indptr: np.ndarray, flat: np.ndarray, n_rows: int, mc: int):
-    """(row_ptr, column ids int32, items of the columns): rows deduplicated, columns = items with count >= mc."""
+    """(row_ptr, column ids int32, items of the columns): rows deduplicated, columns = items with count >= mc.
+
+    The host restatement of ``_frequent_csr_device`` (used by the serving loop's dataset builder)."""
     rid = np.repeat(np.arange(n_rows, dtype=np.int64), np.diff(indptr))
     items, inv = np.unique(flat, return_inverse=True)
     key = rid * max(1, len(items)) + inv
