@@ -338,7 +338,8 @@ def main() -> None:
     ap.add_argument("--tc-elem", type=int, default=17, choices=[1, 2, 9, 10, 17, 18],
                     help="tensor operands: 1 = e4m3, 2 = f16; + 8: the CTA-pair kernel; + 16: the 256 x 256 kernel")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparator")
-    ap.add_argument("--proj-gb", type=float, default=4.0, help="device GB of projected words per chunk")
+    ap.add_argument("--proj-gb", type=float, default=8.0, help="device GB of projected words per chunk")
+    ap.add_argument("--chunk-cands", type=int, default=None, help="candidates per chunk (default: the engine's)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-pipeline", action="store_true",
                     help="project and count chunks in turn on one stream (per-kernel times without overlap)")
@@ -377,8 +378,9 @@ def main() -> None:
     method = args.method or engm.DEFAULT_METHOD
     bv = dense_k2_device(pkg, lib, spec)
     n_rows = spec["n_rows"]
+    extra = {"chunk_cands": args.chunk_cands} if args.chunk_cands else {}
     eng = engm.Engine(form="batched", method=method, tc_elem=args.tc_elem, proj_bytes=int(args.proj_gb * (1 << 30)),
-                      pipeline=not args.no_pipeline)
+                      pipeline=not args.no_pipeline, **extra)
     eng.profile_kernels = True
 
     def one(e):

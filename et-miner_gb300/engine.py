@@ -42,14 +42,14 @@ SMALL_GROUP = 16
 #: Suffixes per tile side of the tile-pair kernel.
 TILE = 64
 #: Candidates per chunk (int32 count + uint8 class each): bounds the level's dense scratch.
-CHUNK_CANDS = 1 << 27
+CHUNK_CANDS = 1 << 28
 #: A group of more than SMALL_GROUP members is counted on its prefix's rows only when the prefix
 #: holds less than this fraction of the transactions.
 PROJ_DENSITY = 0.5
-#: Device bytes of projected suffix words (and row lists) per chunk.
-PROJ_BYTES = 4 << 30
-#: Members per B super-tile of the tensor-core Gram kernel; each super-tile pair (ua <= ub) is two
-#: work items (the two 128-member halves of ua against all 256 members of ub).
+#: Device bytes of projected suffix words per chunk (two such sets alternate between the streams).
+PROJ_BYTES = 8 << 30
+#: Members per block of the tensor-core Gram kernels; a block pair (ua <= ub) is one work item of the
+#: wide and CTA-pair kernels, two of the 128 x 256 kernel (the 128-member halves of ua against ub).
 TC_TILE = 256
 #: Largest group (rows) the tensor-core Gram counts exactly: f32 holds every integer up to 2^24.
 TC_MAX_ROWS = 1 << 24
