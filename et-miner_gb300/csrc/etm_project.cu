@@ -103,15 +103,35 @@ constexpr int P_WARPS = PT / 32;
 constexpr int PROJ_SMEM = STAGE_BYTES * NSTAGE + SEG_W * 8 + LIST_CAP * 2;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+// Bulk (TMA) copies of whole member segments into shared memory, completed on an mbarrier.
+constexpr long long BULK_WAIT_LIMIT = 1LL << 26;
+__device__ int g_proj_status;
+__device__ __forceinline__ void bar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
 }
-__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+__device__ __forceinline__ void bar_expect(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool bar_try(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits (bounded) for the phase of `parity`; false when the limit ran out.
+__device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
+    for (long long n = 0; !bar_try(bar, parity); n++)
+        if (n > BULK_WAIT_LIMIT) return false;
+    return true;
+}
 
 // One block per work entry: the words of every segment's piece, their exclusive prefix (seg_off, n_seg + 1
 // entries per work entry) and the total (out_words).
@@ -164,6 +184,7 @@ struct PassArgs {
     uint64_t* dst;
     int64_t stride, out0;
     uint64_t* park;  // MPI x 4 MAX_CHUNKS words per warp of shared memory
+    uint64_t* bars;  // two mbarriers (shared memory): group slots 0 and 1 of the stage buffers
     int32_t* ids;    // ID_RING member column ids (shared memory)
 };
 
@@ -174,7 +195,7 @@ struct PassArgs {
 // buffer. Per member a word then costs two shared loads, two bit tests and two ballots; members go MPI
 // at a time (independent chains, one block barrier per MPI members); lane 0 parks the words in shared
 // memory and the warp stores them with coalesced stores.
-__device__ __forceinline__ void gather_members(const PassArgs& a) {
+__device__ __forceinline__ bool gather_members(const PassArgs& a, uint32_t& phase) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int m = (int)a.m;
     const int n_chunks = (a.pass_words + 3) >> 2;
@@ -196,20 +217,23 @@ __device__ __forceinline__ void gather_members(const PassArgs& a) {
             valid |= (t < a.pass_words ? 1u : 0u) << i;
         }
     }
-    // Copies: member j's segment words into stage buffer j % NSTAGE, 16 bytes per thread and step, MPI
-    // members per commit group. One group per MPI members (empty past the last member), so the wait
-    // below always leaves NSTAGE / MPI - 2 groups pending and the current members' copies have landed. Member
-    // column ids come from a ring of ID_RING entries in shared memory, refilled half a ring ahead (its
-    // global latency is paid once per ID_RING / 2 members, not per member).
+    // Copies: members t MPI .. t MPI + MPI - 1 (group t) go to group slot t % 2 (stage buffers
+    // (t % 2) MPI ..), each member segment one bulk (TMA) copy issued by thread 0 and completed on the
+    // slot's mbarrier; group t + 1 is issued once every warp is past group t - 1. Member column ids come
+    // from a ring of ID_RING entries in shared memory, refilled half a ring ahead.
     const int32_t* colp = a.rows + a.first * a.width + a.width - 1;
-    const int n16 = a.nw >> 1;
-    const bool odd = (a.nw & 1) && threadIdx.x == 0;
-    auto copy = [&](int j, int buf) {
-        if (j < m) {
+    const uint32_t seg_bytes = (uint32_t)((a.nw + 1) & ~1) * 8;  // whole 16-byte pieces (ld is even)
+    const int n_groups = (m + MPI - 1) / MPI;
+    auto issue = [&](int t) {
+        if (threadIdx.x != 0 || t >= n_groups) return;
+        const int slot = t & 1;
+        const int nv = min(MPI, m - t * MPI);
+        bar_expect(&a.bars[slot], (uint32_t)nv * seg_bytes);
+        for (int v = 0; v < nv; v++) {
+            const int j = t * MPI + v;
             const uint64_t* src = a.fbv + (int64_t)a.ids[j & (ID_RING - 1)] * a.ld + a.w0;
-            uint8_t* d = reinterpret_cast<uint8_t*>(a.stage) + buf * STAGE_BYTES;
-            for (int i = threadIdx.x; i < n16; i += PT) cp_async16(d + 16 * i, src + 2 * i);
-            if (odd) cp_async8(d + 8 * (a.nw - 1), src + a.nw - 1);
+            bulk_copy(reinterpret_cast<uint8_t*>(a.stage) + (slot * MPI + v) * STAGE_BYTES, src, seg_bytes,
+                      &a.bars[slot]);
         }
     };
     auto fill_ids = [&](int j1) {  // members [j1, j1 + ID_RING / 2)
@@ -221,12 +245,7 @@ __device__ __forceinline__ void gather_members(const PassArgs& a) {
     fill_ids(0);
     fill_ids(ID_RING / 2);
     __syncthreads();
-#pragma unroll
-    for (int d = 0; d < NSTAGE - MPI; d += MPI) {
-#pragma unroll
-        for (int v = 0; v < MPI; v++) copy(d + v, d + v);
-        cp_async_commit();
-    }
+    issue(0);
     const uint8_t* sbytes = reinterpret_cast<const uint8_t*>(a.stage);
     uint64_t* park = a.park + warp * MPI * 4 * MAX_CHUNKS;
     const bool my_store = lane < 4 * MAX_CHUNKS && ((valid >> lane) & 1u);
@@ -237,12 +256,17 @@ __device__ __forceinline__ void gather_members(const PassArgs& a) {
         for (int u = 0; u < NSTAGE; u += MPI) {
             const int j = j0 + u;
             if (j >= m) break;
-            cp_async_wait<NSTAGE / MPI - 2>();
-            __syncthreads();  // members j .. j + MPI - 1 visible to all; every warp is past the previous ones
-#pragma unroll
-            for (int v = 0; v < MPI; v++)  // into the buffers of the previous MPI members
-                copy(j + NSTAGE - MPI + v, (u + NSTAGE - MPI + v) % NSTAGE);
-            cp_async_commit();
+            const int slot = u / MPI;  // group j / MPI
+            const bool got = bar_wait(&a.bars[slot], (phase >> slot) & 1u);
+            phase ^= 1u << slot;
+            // Members j .. j + MPI - 1 have landed and every warp is past the previous group (or a wait ran out).
+            if (__syncthreads_or(!got)) {
+                // Give the copies of this group a second bounded wait before the block stops.
+                bar_wait(&a.bars[slot], (phase >> slot) & 1u ^ 1u);
+                if (threadIdx.x == 0) atomicExch(&g_proj_status, ETM_ETIMEOUT);
+                return false;
+            }
+            issue(j / MPI + 1);  // into the other slot
             if ((j & (ID_RING / 2 - 1)) == 0 && j > 0) fill_ids(j + ID_RING / 2);
             const uint8_t* sa = sbytes + u * STAGE_BYTES;
 #pragma unroll
@@ -275,7 +299,7 @@ __device__ __forceinline__ void gather_members(const PassArgs& a) {
             __syncwarp();
         }
     }
-    cp_async_wait<0>();
+    return true;
 }
 
 // Unit (segment s, work entry wi): the prefix words of the segment, the list of its prefix rows (local
@@ -300,9 +324,18 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
     __shared__ uint64_t park[P_WARPS * MPI * 4 * MAX_CHUNKS];
     __shared__ int32_t ids[ID_RING];
     __shared__ int64_t next_sh;
+    __shared__ __align__(8) uint64_t bars[2];
     const int plen = width - 1;
     const int64_t total = n_seg * n_work;
-    if (threadIdx.x < 2 * NSTAGE)  // the zero pads after the stage buffers (cp.async never writes them)
+    if (threadIdx.x == 0) {
+        bar_init(&bars[0]);
+        bar_init(&bars[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    uint32_t phase = 0;  // bit s: parity of the next phase of group slot s
+    bool stop = false;
+    if (threadIdx.x < 2 * NSTAGE)  // the zero pads after the stage buffers (the copies never write them)
         reinterpret_cast<uint64_t*>(psmem + (threadIdx.x >> 1) * STAGE_BYTES + SEG_W * 8)[threadIdx.x & 1] = 0ULL;
     // Units in segment-major order; with a work counter each CTA claims the next unclaimed one.
     auto next_unit = [&](int64_t q) -> int64_t {
@@ -365,11 +398,14 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
                 list[((x >> 6) << 6) + ((x & 31) << 1) + ((x >> 5) & 1)] = 0;
             __syncthreads();
             const PassArgs pa{fbv, ld, rows, width, first, m, w0, nw, stage, reinterpret_cast<const uint32_t*>(list),
-                              pass_rows, pass_words, dst, stride, p0 >> 6, park, ids};
-            gather_members(pa);
-            cp_async_wait<0>();
+                              pass_rows, pass_words, dst, stride, p0 >> 6, park, bars, ids};
+            if (!gather_members(pa, phase)) {
+                stop = true;
+                break;
+            }
             __syncthreads();  // the next pass rewrites the list
         }
+        if (stop) break;  // a bulk copy did not land within its bounded wait (block-uniform)
         if (s == n_seg - 1) {
             // Zero the words after the last piece, up to the member stride.
             const int64_t used = so[n_seg];
