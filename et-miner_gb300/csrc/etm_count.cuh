@@ -15,6 +15,8 @@ int count_tiles_proj_popcount(const uint64_t* cbuf, const int64_t* cbase, const 
                               const int64_t* work_off, int64_t n_work, int64_t chunk_base, const uint8_t* cls,
                               int32_t* out, cudaStream_t s);
 
+int proj_status_take(cudaStream_t s, int* out);
+
 int gram_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
             const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
             int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t elem, int32_t* out,

@@ -1135,6 +1135,11 @@ extern "C" int etm_device_status(void* stream) {
         ETM_CUDA(cudaMemcpyToSymbolAsync(g_tc_status, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, as_stream(stream)));
         ETM_CUDA(cudaStreamSynchronize(as_stream(stream)));
         etm::set_error("a tensor-core counting kernel gave up a bounded wait (status %d)", v);
+        return v;
     }
-    return v;
+    int p = 0;
+    const int st = etm::proj_status_take(as_stream(stream), &p);
+    if (st != ETM_OK) return st;
+    if (p != 0) etm::set_error("the projection gave up a bounded wait for its bulk copies (status %d)", p);
+    return p;
 }

@@ -421,6 +421,25 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
 
 }  // namespace
 
+namespace etm {
+
+// The projection's status word (ETM_ETIMEOUT after a bulk copy outlived its bounded wait), read and
+// cleared on `s`.
+int proj_status_take(cudaStream_t s, int* out) {
+    int v = 0;
+    ETM_CUDA(cudaMemcpyFromSymbolAsync(&v, g_proj_status, sizeof(int), 0, cudaMemcpyDeviceToHost, s));
+    ETM_CUDA(cudaStreamSynchronize(s));
+    if (v != 0) {
+        const int zero = 0;
+        ETM_CUDA(cudaMemcpyToSymbolAsync(g_proj_status, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s));
+        ETM_CUDA(cudaStreamSynchronize(s));
+    }
+    *out = v;
+    return ETM_OK;
+}
+
+}  // namespace etm
+
 extern "C" int etm_prefix_counts(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
                                  const int64_t* grp_first, const int64_t* work_groups, int64_t n_work,
                                  int64_t* out_counts, void* stream) {

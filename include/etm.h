@@ -260,8 +260,9 @@ int etm_count_tiles_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t
                        const uint8_t* cls, int32_t elem, int32_t* out_counts, int64_t* work_counter, void* stream);
 
 /*
- * Reads and clears the device status word the tensor-core kernels raise when a
- * bounded wait gives up (synchronizes `stream`). Returns 0, or ETM_ETIMEOUT.
+ * Reads and clears the device status words the tensor-core kernels and the
+ * projection (its bulk copies) raise when a bounded wait gives up
+ * (synchronizes `stream`). Returns 0, or ETM_ETIMEOUT.
  */
 int etm_device_status(void* stream);
 
