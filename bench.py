@@ -52,9 +52,9 @@ WORKLOADS = {
 #: dram__bytes_write.sum,gpu__time_duration.sum --clock-control none -k "regex:gram_wide_kernel|project_seg_kernel"
 #: python bench.py --workload dense_k2_mid --steps 1 --warmup 1 --no-plain --no-cpu --proj-gb 1
 #: --chunk-cands 134217728: per mine
-#: 16.21 GB against 12.66 GB for the Gram, 19.41 GB against 170.35 GB for the projection); the roofline's
+#: 16.21 GB against 12.66 GB for the Gram, 19.63 GB against 170.35 GB for the projection); the roofline's
 #: ``traffic`` scales it to the bench's own launches by their algorithmic bytes.
-DRAM_PER_ALGORITHMIC_BYTE = {"gram_tc": 16.21 / 12.66, "project": 19.41 / 170.35}
+DRAM_PER_ALGORITHMIC_BYTE = {"gram_tc": 16.21 / 12.66, "project": 19.63 / 170.35}
 
 
 def _peaks() -> dict:
