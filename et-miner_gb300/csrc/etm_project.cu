@@ -10,8 +10,8 @@
 //                        row its word offset
 //   3. projection:       per (segment, group): the segment's prefix rows listed
 //                        in shared memory; per member its segment words staged
-//                        in shared memory with cp.async and gathered at the
-//                        listed rows, 64 per word by two warp ballots
+//                        in shared memory by a TMA bulk copy and gathered at
+//                        the listed rows, 64 per word by two warp ballots
 //   (prefix rows:        the ascending transaction ids of the prefix AND, kept
 //                        as an entry point for callers that want the tidset)
 //
@@ -304,8 +304,8 @@ __device__ __forceinline__ bool gather_members(const PassArgs& a, uint32_t& phas
 
 // Unit (segment s, work entry wi): the prefix words of the segment, the list of its prefix rows (local
 // row ids, 16 bits), both in shared memory, then for every member its segment words staged in
-// shared memory (cp.async, NSTAGE buffers, NSTAGE - 1 members ahead) and gathered at the listed rows
-// with two ballots per 64 rows. Warp w writes a contiguous run of output words, one per lane.
+// shared memory (one bulk copy per member, NSTAGE buffers in two slots of MPI, the next slot's copies
+// in flight while one slot is gathered) and gathered at the listed rows with two ballots per 64 rows.
 __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __restrict__ fbv, int64_t ld,
                                                          int64_t n_words, const int32_t* __restrict__ rows,
                                                          int width, const int64_t* __restrict__ grp_first,
