@@ -194,7 +194,7 @@ def _python_rows(rows) -> tuple[np.ndarray, np.ndarray, np.dtype]:
 def _frequent_csr(indptr: np.ndarray, flat: np.ndarray, n_rows: int, mc: int):
     """(row_ptr, column ids int32, items of the columns): rows deduplicated, columns = items with count >= mc.
 
-    The host restatement of ``_frequent_csr_device`` (used by the serving loop's dataset builder)."""
+    The host restatement of ``_frequent_csr_device`` (the tests check one against the other)."""
     rid = np.repeat(np.arange(n_rows, dtype=np.int64), np.diff(indptr))
     items, inv = np.unique(flat, return_inverse=True)
     key = rid * max(1, len(items)) + inv

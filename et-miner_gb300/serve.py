@@ -73,13 +73,18 @@ class Result:
 
 
 def dataset_from_transactions(indptr: np.ndarray, items: np.ndarray, device=None) -> Dataset:
-    """Build a resident dataset on the device (etm_build_bitvecs) from a transaction CSR."""
-    from .api import _frequent_csr, build_device_bitvecs
+    """Build a resident dataset on the device from a transaction CSR: the item columns (deduplicated per
+    row, in ascending id order) and their bitvectors (etm_build_bitvecs), all on the device."""
+    import torch
 
+    from .api import _bitvecs_of_device_csr, _frequent_csr_device
+
+    dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
     n_rows = len(indptr) - 1
-    row_ptr, cols, col_items = _frequent_csr(indptr, np.asarray(items), n_rows, 1)
-    bv = build_device_bitvecs(row_ptr, cols, len(col_items), n_rows, device)
-    counts = np.bincount(cols, minlength=len(col_items)).astype(np.int64)
+    row_ptr, cols, col_items, _ = _frequent_csr_device(np.asarray(indptr, np.int64), np.asarray(items), n_rows, 1, dev)
+    with torch.cuda.device(dev):
+        bv = _bitvecs_of_device_csr(row_ptr, cols, len(col_items), n_rows)
+    counts = torch.bincount(cols.long(), minlength=len(col_items)).cpu().numpy().astype(np.int64)
     return Dataset(bv, col_items.astype(np.int64), n_rows, counts)
 
 
