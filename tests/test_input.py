@@ -31,3 +31,25 @@ def test_device_frequent_csr_matches_host(pkg, wide, mc):
     assert np.array_equal(rp_d.numpy(), rp_h)
     assert np.array_equal(cols_d.numpy(), cols_h)
     assert np.array_equal(row_len, np.diff(rp_h))
+
+
+@pytest.mark.parametrize("kw,exc,match", [
+    (dict(min_support=1.5), ValueError, r"\[0.0, 1.0\]"),
+    (dict(min_support="0.1"), TypeError, "numeric"),
+    (dict(min_support=True), TypeError, "numeric"),
+    (dict(min_support=0.1, max_length=0), ValueError, ">= 1"),
+    (dict(min_support=0.1, max_length=2.0), TypeError, "int or None"),
+    (dict(min_support=0.1, batch_size=0), ValueError, ">= 1"),
+    (dict(min_support=0.1, sparse=True), ValueError, "sparse= was removed"),
+    (dict(min_support=0.1, gpu_resident=True), ValueError, "gpu_resident"),
+    (dict(min_support=0.1, sparse_from_k=3), ValueError, "sparse_from_k"),
+    (dict(min_support=0.1, prune_apriori=False), ValueError, "prune_apriori"),
+    (dict(min_support=0.1, streaming=True), ValueError, "streaming"),
+    (dict(min_support=0.1, output_dir="/tmp/x"), ValueError, "output_dir"),
+    (dict(min_support=0.1, anchor_items={1}), ValueError, "anchor_items"),
+])
+def test_parameter_checks_need_no_gpu(pkg, kw, exc, match):
+    """The reference's parameter checks (core/apriori.py:64-106) and the rejected routes raise before any
+    device work, with the reference's exception types."""
+    with pytest.raises(exc, match=match):
+        pkg.apriori([[1, 2], [2, 3]], use_gpu=True, **kw)
