@@ -251,6 +251,92 @@ def run_reference(args, spec) -> None:
     print(json.dumps(line), flush=True)
 
 
+TX_METRIC = "apriori(transactions) seconds, plain small (60K x 1,000, s=0.01), exact counts"
+#: Workloads mined through the transactions route (host CSR in, result frame out).
+TX_WORKLOADS = {
+    "plain_small_tx": dict(gen="plain_small", n_rows=60_000, n_items=1_000, min_support=0.01, max_length=None, seed=0),
+}
+
+
+def run_transactions(args) -> None:
+    """The transactions route on the plain small workload (60K rows x 1,000 Zipf(1.1) items, s=0.01):
+    seconds per ``apriori(transactions, use_gpu=True)`` call (transaction CSR on the host in, result frame
+    out), the kernels it ran, exactness against the CPU oracle, and the oracle's whole mine of the same
+    input timed beside it (this workload is small enough for the oracle to run in full)."""
+    import torch
+
+    from oracle import miner
+
+    spec = TX_WORKLOADS[args.workload]
+    pkg = _pkg()
+    syn = pkg.synthetic
+    t = getattr(syn, spec["gen"])(seed=spec["seed"])
+    n_rows = t.n_rows
+
+    def cpu_mine():
+        t0 = time.perf_counter()
+        res, col_items = miner.mine_transactions(t.indptr, t.items, n_rows, spec["min_support"], spec["max_length"])
+        return time.perf_counter() - t0, miner.canonical(res.levels, col_items)
+
+    if args.impl == "reference":
+        cpu_s, _ = cpu_mine()
+        base = {"value": cpu_s, "unit": "s", "cores": 1, "kind": "port",
+                "sample": "oracle/miner.py mine_transactions: the whole mine of the workload, one core"}
+        print(json.dumps({"impl": "reference", "metric": TX_METRIC, "value": cpu_s, "unit": "s", "n_gpus": args.gpus,
+                          "steps": 1, "warmup": 0, "ms_per_step": cpu_s * 1e3, "higher_is_better": False,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+                          "config": {"workload": args.workload, **spec}, "cpu_baseline": base,
+                          "e2e": {"value": cpu_s, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+              flush=True)
+        return
+    pkg.build_library()
+    from importlib import import_module
+
+    engm = import_module(pkg.__name__ + ".engine")
+    eng = engm.Engine()
+    eng.profile_kernels = True
+    levels = []
+
+    def call():
+        levels.clear()
+        return pkg.apriori(t, min_support=spec["min_support"], max_length=spec["max_length"], use_gpu=True,
+                           engine=eng, warn_complexity=False,
+                           level_callback=lambda k, nc, nf, ms: levels.append({"k": k, "candidates": nc,
+                                                                               "frequent": nf}))
+
+    for _ in range(max(1, args.warmup)):
+        df = call()
+    torch.cuda.synchronize()
+    eng.reset_kernel_times()
+    launches0 = eng.launches
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        df = call()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    kern = eng.kernel_report()
+    cpu_s, want = cpu_mine()
+    got = pkg.result_pairs(df, n_rows)
+    n_sets = len(got)
+    n_vals = sum(len(s) for s, _ in got)
+    line = {
+        "metric": TX_METRIC, "value": dt, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded plain_small generator, host CSR)",
+        "config": {"workload": args.workload, **spec, "route": "transactions"},
+        "levels": list(levels), "exact": got == want, "itemsets": n_sets,
+        "e2e": {"value": dt, "unit": "s", "h2d_bytes_per_step": int(t.indptr.nbytes + t.items.nbytes),
+                "d2h_bytes_per_step": 8 * n_vals + 16 * n_sets + 8},
+        "kernels": kern, "gpu_launches": (eng.launches - launches0) // args.steps,
+        "cpu_baseline": {"value": cpu_s, "unit": "s", "cores": 1, "kind": "port",
+                         "sample": "oracle/miner.py mine_transactions: the whole mine of the workload, one core"},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_serving(args) -> None:
     """Serving workload: 256 Poisson-arriving requests over 8 resident datasets, p50/p99 latency."""
     import torch
@@ -331,7 +417,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="dense_k2", choices=sorted(WORKLOADS) + ["serving"])
+    ap.add_argument("--workload", default="dense_k2", choices=sorted(WORKLOADS) + sorted(TX_WORKLOADS) + ["serving"])
     ap.add_argument("--slots", type=int, default=4, help="serving: requests on the GPU at once")
     ap.add_argument("--serving-scale", type=float, default=1.0, help="serving: dataset row scale")
     ap.add_argument("--serving-requests", type=int, default=256)
@@ -351,6 +437,10 @@ def main() -> None:
             return
         if int(os.environ.get("RANK", "0")) == 0:
             run_serving(args)
+        return
+    if args.workload in TX_WORKLOADS:
+        if int(os.environ.get("RANK", "0")) == 0:
+            run_transactions(args)
         return
     spec = WORKLOADS[args.workload]
     rank = int(os.environ.get("RANK", "0"))
