@@ -92,6 +92,7 @@ SIGNATURES: dict[str, tuple] = {
     "etm_popcount_cols": (ctypes.c_int, [_P, _I64, _I64, _I64, _P, _P]),
     "etm_gather_cols": (ctypes.c_int, [_P, _I64, _P, _I32, _I64, _P, _I64, _P]),
     "etm_synth_bernoulli": (ctypes.c_int, [_P, _I32, _I64, _U64, _P, _I64, _P]),
+    "etm_synth_patterns": (ctypes.c_int, [_P, _I32, _P, _I32, _P, _P, _I32, _U64, _I32, _I64, _U64, _P, _I64, _P]),
     "etm_level_groups": (ctypes.c_int, [_P, _I64, _I32, _P, _P, _P, _P, _P, _I64, _P]),
     "etm_classify": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _P, _P, _I64, _I64, _I32, _P, _P, _P]),
     "etm_count_tiles": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P]),
@@ -105,6 +106,10 @@ SIGNATURES: dict[str, tuple] = {
     "etm_project": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "etm_count_tiles_proj": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P]),
     "etm_count_tiles_tc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _P, _I32, _P, _P, _P]),
+    "etm_count_tiles_tc_sel": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _P, _I32, _I32, _P,
+                                              _P, _P, _P]),
+    "etm_gram_block_members": (ctypes.c_int, [_I32]),
+    "etm_set_wait_limits": (ctypes.c_int, [_I64, _I64]),
     "etm_device_status": (ctypes.c_int, [_P]),
     "etm_level_compact": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _P, _P, _P, _I64, _I64, _I32, _P, _P, _I64, _P, _P, _I64, _P]),
     "etm_level_compact_static": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _P, _P, _P, _I64, _I64, _I32, _P, _P, _I64, _P, _P]),

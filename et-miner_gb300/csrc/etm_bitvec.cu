@@ -132,7 +132,64 @@ __global__ void synth_bernoulli_kernel(const uint64_t* __restrict__ thr, int32_t
     }
 }
 
+// Rows built from planted patterns, one thread per row (the deep sparse workload's generator, defined by
+// bit_hash so the host restates it exactly). Stream ids of the draws: 1 the length, 2 + p the p-th
+// pattern, 64 + 16 p + q the keep draw of item q of pattern p, 4096 + t the t-th noise draw.
+constexpr int SYN_MAX_LEN = 64;
+__global__ void synth_patterns_kernel(const uint64_t* __restrict__ len_thr, int32_t n_len,
+                                      const uint64_t* __restrict__ pat_thr, int32_t n_pat,
+                                      const int64_t* __restrict__ pat_ptr, const int32_t* __restrict__ pat_items,
+                                      int32_t per_row, uint64_t keep_thr, int32_t n_items, int64_t n_rows,
+                                      uint64_t seed, unsigned long long* __restrict__ out, int64_t ld) {
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += (int64_t)gridDim.x * blockDim.x) {
+        // Length: 1 + the number of cdf thresholds the draw reaches, at most n_len (<= SYN_MAX_LEN).
+        const uint64_t hl = bit_hash(seed, 1, r);
+        int len = 1;
+        while (len - 1 < n_len && hl >= len_thr[len - 1]) ++len;
+        int32_t items[SYN_MAX_LEN];
+        int n = 0;
+        for (int p = 0; p < per_row && n < len; p++) {
+            const uint64_t hp = bit_hash(seed, 2 + p, r);
+            int j = 0;
+            while (j < n_pat - 1 && hp >= pat_thr[j]) ++j;
+            for (int64_t q = pat_ptr[j]; q < pat_ptr[j + 1] && n < len; q++) {
+                if (bit_hash(seed, 64 + 16 * p + (q - pat_ptr[j]), r) >= keep_thr) continue;
+                const int32_t x = pat_items[q];
+                bool dup = false;
+                for (int e = 0; e < n; e++) dup |= items[e] == x;
+                if (!dup) items[n++] = x;
+            }
+        }
+        for (int t = 0; n < len && t < 65536; t++) {
+            const int32_t x = (int32_t)(bit_hash(seed, 4096 + t, r) % (uint64_t)n_items);
+            bool dup = false;
+            for (int e = 0; e < n; e++) dup |= items[e] == x;
+            if (!dup) items[n++] = x;
+        }
+        const unsigned long long bit = 1ULL << (r & 63);
+        for (int e = 0; e < n; e++) atomicOr(out + (int64_t)items[e] * ld + (r >> 6), bit);
+    }
+}
+
 }  // namespace
+
+extern "C" int etm_synth_patterns(const uint64_t* len_thr, int32_t n_len, const uint64_t* pat_thr, int32_t n_pat,
+                                  const int64_t* pat_ptr, const int32_t* pat_items, int32_t per_row,
+                                  uint64_t keep_thr, int32_t n_items, int64_t n_rows, uint64_t seed, uint64_t* out_bv,
+                                  int64_t ld, void* stream) {
+    ETM_REQUIRE(ld >= (n_rows + 63) / 64 && n_items > 0 && n_rows >= 0, ETM_EINVAL, "etm_synth_patterns: bad sizes");
+    ETM_REQUIRE(n_len >= 0 && n_len < SYN_MAX_LEN && n_pat >= 1 && per_row >= 0 && per_row <= 60, ETM_EINVAL,
+                "etm_synth_patterns: n_len must be < %d, n_pat >= 1, per_row in 0..60", SYN_MAX_LEN);
+    cudaStream_t s = as_stream(stream);
+    ETM_CUDA(cudaMemsetAsync(out_bv, 0, (size_t)n_items * ld * 8, s));
+    if (n_rows == 0) return ETM_OK;
+    const int blocks = (int)min64(ceil_div<int64_t>(n_rows, 256), (int64_t)max(1, sm_count()) * 32);
+    synth_patterns_kernel<<<blocks, 256, 0, s>>>(len_thr, n_len, pat_thr, n_pat, pat_ptr, pat_items, per_row, keep_thr,
+                                                 n_items, n_rows, seed, reinterpret_cast<unsigned long long*>(out_bv),
+                                                 ld);
+    ETM_LAUNCHED("synth_patterns");
+    return ETM_OK;
+}
 
 extern "C" int etm_build_bitvecs(const int64_t* row_ptr, const int32_t* ids, int64_t nnz, const int32_t* lut,
                                  int64_t lut_size, int64_t n_rows, int64_t n_cols, int64_t ld, uint64_t* out_bv,

@@ -18,6 +18,8 @@
 // after which the tile-pair kernel counts the group on words that hold only
 // the prefix's rows: a group whose prefix holds a fraction d of the rows
 // costs d of the AND+popcount work it would cost on the full bitvectors.
+#include <atomic>
+
 #include "etm_count.cuh"
 #include "etm_scan.cuh"
 
@@ -104,8 +106,16 @@ constexpr int PROJ_SMEM = STAGE_BYTES * NSTAGE + SEG_W * 8 + LIST_CAP * 2;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 // Bulk (TMA) copies of whole member segments into shared memory, completed on an mbarrier.
-constexpr long long BULK_WAIT_LIMIT = 1LL << 26;
+// Every wait for them is bounded in time (%globaltimer).
+constexpr uint64_t BULK_WAIT_NS = 2000000000ull;
+// Limit of the first wait for a group's copies (a test sets 0 to drive the give-up path).
+std::atomic<uint64_t> g_proj_first_wait_ns{BULK_WAIT_NS};
 __device__ int g_proj_status;
+__device__ __forceinline__ uint64_t now_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 __device__ __forceinline__ void bar_init(uint64_t* bar) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
 }
@@ -126,10 +136,14 @@ __device__ __forceinline__ bool bar_try(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Waits (bounded) for the phase of `parity`; false when the limit ran out.
-__device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
-    for (long long n = 0; !bar_try(bar, parity); n++)
-        if (n > BULK_WAIT_LIMIT) return false;
+// Waits for the phase of `parity`; false when `limit_ns` ran out first (a limit of 0 gives up at once:
+// the give-up path's test hook).
+__device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+    if (limit_ns == 0) return false;
+    if (bar_try(bar, parity)) return true;
+    const uint64_t t0 = now_ns();
+    while (!bar_try(bar, parity))
+        if (now_ns() - t0 > limit_ns) return false;
     return true;
 }
 
@@ -186,6 +200,7 @@ struct PassArgs {
     uint64_t* park;  // MPI x 4 MAX_CHUNKS words per warp of shared memory
     uint64_t* bars;  // two mbarriers (shared memory): group slots 0 and 1 of the stage buffers
     int32_t* ids;    // ID_RING member column ids (shared memory)
+    uint64_t first_wait_ns;  // limit of each wait for a group's copies
 };
 
 // Every member of the group through the stage buffers, for one pass of listed rows. The pass's output
@@ -257,13 +272,17 @@ __device__ __forceinline__ bool gather_members(const PassArgs& a, uint32_t& phas
             const int j = j0 + u;
             if (j >= m) break;
             const int slot = u / MPI;  // group j / MPI
-            const bool got = bar_wait(&a.bars[slot], (phase >> slot) & 1u);
+            const bool got = bar_wait(&a.bars[slot], (phase >> slot) & 1u, a.first_wait_ns);
             phase ^= 1u << slot;
             // Members j .. j + MPI - 1 have landed and every warp is past the previous group (or a wait ran out).
             if (__syncthreads_or(!got)) {
-                // Give the copies of this group a second bounded wait before the block stops.
-                bar_wait(&a.bars[slot], (phase >> slot) & 1u ^ 1u);
-                if (threadIdx.x == 0) atomicExch(&g_proj_status, ETM_ETIMEOUT);
+                // Only this slot's copies can be in flight (the other slot's were consumed before these were
+                // issued): every thread waits for them, bounded, before the block stops. If even that wait
+                // runs out, the status says so: copies may still land in this SM's shared memory, and the
+                // caller must stop using the device.
+                const bool drained = got || bar_wait(&a.bars[slot], (phase >> slot) & 1u ^ 1u, BULK_WAIT_NS);
+                if (threadIdx.x == 0) atomicExch(&g_proj_status, drained ? ETM_ETIMEOUT : ETM_EUNSAFE);
+                __syncthreads();
                 return false;
             }
             issue(j / MPI + 1);  // into the other slot
@@ -315,7 +334,8 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
                                                          const int64_t* __restrict__ cbase,
                                                          const int64_t* __restrict__ cld,
                                                          uint64_t* __restrict__ cbuf,
-                                                         unsigned long long* __restrict__ work_counter) {
+                                                         unsigned long long* __restrict__ work_counter,
+                                                         uint64_t first_wait_ns) {
     extern __shared__ __align__(16) uint8_t psmem[];
     uint64_t* stage = reinterpret_cast<uint64_t*>(psmem);  // NSTAGE x (SEG_W member words + zero pad)
     uint64_t* pw = reinterpret_cast<uint64_t*>(psmem + NSTAGE * STAGE_BYTES);  // SEG_W prefix words
@@ -398,7 +418,7 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
                 list[((x >> 6) << 6) + ((x & 31) << 1) + ((x >> 5) & 1)] = 0;
             __syncthreads();
             const PassArgs pa{fbv, ld, rows, width, first, m, w0, nw, stage, reinterpret_cast<const uint32_t*>(list),
-                              pass_rows, pass_words, dst, stride, p0 >> 6, park, bars, ids};
+                              pass_rows, pass_words, dst, stride, p0 >> 6, park, bars, ids, first_wait_ns};
             if (!gather_members(pa, phase)) {
                 stop = true;
                 break;
@@ -422,6 +442,8 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
 }  // namespace
 
 namespace etm {
+
+void proj_set_first_wait(int64_t ns) { g_proj_first_wait_ns.store(ns < 0 ? BULK_WAIT_NS : (uint64_t)ns); }
 
 // The projection's status word (ETM_ETIMEOUT after a bulk copy outlived its bounded wait), read and
 // cleared on `s`.
@@ -500,7 +522,8 @@ extern "C" int etm_project(const uint64_t* fbv, int64_t ld, int64_t n_words, con
     project_seg_kernel<<<grid, PT, PROJ_SMEM, as_stream(stream)>>>(fbv, ld, n_words, rows, width, grp_first, grp_size,
                                                                    work_groups, n_work, n_seg, seg_off, cbase, cld,
                                                                    cbuf,
-                                                                   reinterpret_cast<unsigned long long*>(work_counter));
+                                                                   reinterpret_cast<unsigned long long*>(work_counter),
+                                                                   g_proj_first_wait_ns.load());
     ETM_LAUNCHED("project");
     return ETM_OK;
 }

@@ -48,8 +48,8 @@ CHUNK_CANDS = 1 << 28
 PROJ_DENSITY = 0.5
 #: Device bytes of projected suffix words per chunk (two such sets alternate between the streams).
 PROJ_BYTES = 8 << 30
-#: Members per block of the tensor-core Gram kernels; a block pair (ua <= ub) is one work item of the
-#: wide and CTA-pair kernels, two of the 128 x 256 kernel (the 128-member halves of ua against ub).
+#: Members per block of the tensor-core Gram kernel (e4m3 and f16 operands; packed e2m1 blocks hold 240):
+#: a block pair (ua <= ub) is one work item.
 TC_TILE = 256
 #: Largest group (rows) the tensor-core Gram counts exactly: f32 holds every integer up to 2^24.
 TC_MAX_ROWS = 1 << 24
@@ -81,18 +81,23 @@ def proj_stride(pcnt: np.ndarray, n_words: int) -> np.ndarray:
     return np.maximum(32, ((np.asarray(pcnt, np.int64) + 63) // 64 + n_seg + 31) // 32 * 32)
 
 
-TC_PAIR = 8  # ETM_TC_PAIR: the CTA-pair Gram kernel (tc_elem flag)
-TC_WIDE = 16  # ETM_TC_WIDE: the 256 x 256 single-CTA Gram kernel (tc_elem flag)
-#: e4m3 operands on the wide kernel: the fastest exact form measured on GB300.
+TC_MXF4 = 4  # ETM_TC_MXF4: packed e2m1 operands under kind::mxf4 (tc_elem code)
+TC_WIDE = 16  # ETM_TC_WIDE: accepted in tc_elem and ignored (every code runs the block-pair kernel)
+#: e4m3 operands: the fastest exact form measured on GB300.
 DEFAULT_TC_ELEM = 1 | TC_WIDE
 
 
+def tc_block(tc_elem: int = DEFAULT_TC_ELEM) -> int:
+    """Members per block of the Gram kernel for an element code: 240 for packed e2m1, else 256."""
+    return 240 if (tc_elem & ~TC_WIDE) == TC_MXF4 else TC_TILE
+
+
 def _tile_items(m: np.ndarray, method: int, tc_elem: int = DEFAULT_TC_ELEM) -> np.ndarray:
-    """Work items of groups of m members: 64 x 64 tile-pairs (popcount), 128 x 256 Gram items (tensor)
-    or 256 x 256 block pairs (tensor, CTA-pair kernel)."""
+    """Work items of groups of m members: 64 x 64 tile-pairs (popcount) or Gram block pairs ua <= ub (tensor)."""
     if method == 1:
-        nb = (m + TC_TILE - 1) // TC_TILE
-        return nb * (nb + 1) // 2 if tc_elem & (TC_PAIR | TC_WIDE) else nb * (nb + 1)
+        t = tc_block(tc_elem)
+        nb = (m + t - 1) // t
+        return nb * (nb + 1) // 2
     nt = (m + TILE - 1) // TILE
     return nt * (nt + 1) // 2
 
@@ -279,7 +284,9 @@ class Engine:
         self.project = bool(project)
         self.proj_density = float(proj_density)
         self.proj_bytes = int(proj_bytes)
-        #: Tensor-core operand element: 2 = f16 (kind::f16), 1 = e4m3 (kind::f8f6f4).
+        #: Tensor-core operand element: 1 = e4m3 (kind::f8f6f4), 2 = f16 (kind::f16), 4 = packed e2m1 (kind::mxf4).
+        if (int(tc_elem) & ~TC_WIDE) not in (1, 2, TC_MXF4):
+            raise ValueError(f"tc_elem must be 1 (e4m3), 2 (f16) or 4 (e2m1), optionally | 16; got {tc_elem}")
         self.tc_elem = int(tc_elem)
         #: Batched form: project chunk c+1 on a side stream while chunk c is counted.
         self.pipeline = bool(pipeline)
@@ -289,7 +296,6 @@ class Engine:
         self.k3_rows_max_r = K3_ROWS_MAX_R
         self._k2_rows = None
         self._rows_input = None
-        self._rows_input = None
         #: Counting settings chosen per level shape by timing (None: the fixed defaults).
         self.autotuner = Autotuner() if autotune is True else (autotune or None)
         self.scratch = _Scratch(self.device)
@@ -298,10 +304,13 @@ class Engine:
         self.profile_kernels = False
         self._events: list[tuple] = []
         self.used_tensor = False
+        #: Set when a kernel with bounded device waits (the Gram, the projection) ran since the last status read.
+        self._waits_pending = False
+        self._side: torch.cuda.Stream | None = None
 
     def _side_stream(self) -> torch.cuda.Stream:
         """The stream projection runs on beside the counting kernels (created on first use)."""
-        if getattr(self, "_side", None) is None:
+        if self._side is None:
             self._side = torch.cuda.Stream(device=self.device)
         return self._side
 
@@ -420,6 +429,7 @@ class Engine:
                                                        _p(grp_size), _p(wg), n, _p(seg_off), _p(cbase), _p(cld),
                                                        _p(cbuf), _p(proj_counter), _stream()))
         check(st, "etm_project")
+        self._waits_pending = True
         self.launches += 2
         return dict(d=d, cbuf=cbuf, cbase=cbase, cwords=cwords, cld=cld, wg=wg, wo=wo, n=n, n_tiles=int(toff[-1]),
                     nbytes=int((m * ((cnt + 63) // 64)).sum() * 8),
@@ -453,6 +463,7 @@ class Engine:
                 base, _p(cls), self.tc_elem, _p(counts), _p(counter), _stream()), flops=2 * macs)
             check(st, "etm_count_tiles_tc")
             self.used_tensor = True
+            self._waits_pending = True
         else:
             st = self._launch("count_tiles_proj", nbytes, lambda: self.lib.etm_count_tiles_proj(
                 _p(cbuf), _p(cbase), _p(cwords), _p(cld), _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, base,
@@ -718,11 +729,24 @@ class Engine:
                 acc.fill_(n_out)
             n_out = new_total
             stats.n_chunks += 1
-        if self.used_tensor:
-            st = self.lib.etm_device_status(_stream())
-            if st != 0:
-                raise RuntimeError(f"tensor-core counting failed: {self.lib.etm_last_error().decode()}")
+        self.check_device_status()
         return Level(out_rows[:n_out], out_counts[:n_out])
+
+    def check_device_status(self) -> None:
+        """Raise if a Gram or projection launch since the last check gave up a bounded device wait.
+
+        The kernels record the give-up in device status words instead of hanging; their counts are then
+        incomplete, so the level is not returned. The projection's give-up leaves the device in an unknown
+        state (bulk copies may still be landing): the caller should stop using the device.
+        """
+        if not self._waits_pending:
+            return
+        if self._side is not None:
+            torch.cuda.current_stream().wait_stream(self._side)
+        self._waits_pending = False
+        st = self.lib.etm_device_status(_stream())
+        if st != 0:
+            raise RuntimeError(f"device counting failed: {self.lib.etm_last_error().decode()}")
 
     def finish_level(self, new: Level, gen: Level, track_free: bool, prune: bool) -> Level:
         """Free flags against the generating level; under the free-set prune keep the free rows

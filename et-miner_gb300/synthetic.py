@@ -167,6 +167,118 @@ def deep_sparse(
     return Transactions(indptr, val.astype(np.int64), n_rows)
 
 
+@dataclass(frozen=True)
+class PatternSpec:
+    """Tables of the hash-defined planted-pattern workload (the deep sparse configuration on the device).
+
+    ``len_thr[i]`` = floor(P(1 + Poisson(mean_len) <= i + 1) * 2^64) for i < n_len; ``pat_thr[j]`` =
+    floor(cdf_j * 2^64) of the exponential pattern weights; patterns as a CSR (``pat_ptr``, ``pat_items``:
+    lengths min(1 + Poisson(9), 16), Zipf(1.0) items without repeats); ``keep_thr`` = floor(0.7 * 2^64).
+    """
+
+    len_thr: np.ndarray
+    pat_thr: np.ndarray
+    pat_ptr: np.ndarray
+    pat_items: np.ndarray
+    keep_thr: int
+    n_items: int
+    per_row: int
+    hash_seed: int
+
+
+def _u64_thresholds(cdf: np.ndarray) -> np.ndarray:
+    """floor(c * 2^64) of probabilities in [0, 1], exact in integers (1.0 maps to 2^64 - 1)."""
+    from math import frexp
+
+    out = np.empty(len(cdf), dtype=np.uint64)
+    for i, c in enumerate(np.asarray(cdf, dtype=np.float64).tolist()):
+        m, e = frexp(c)  # c = m * 2^e, m in [0.5, 1): floor(c * 2^64) = floor(m * 2^53 * 2^(11 + e))
+        mant = int(m * 2**53)
+        v = mant << (11 + e) if e >= -11 else mant >> (-(11 + e))
+        out[i] = min(v, 2**64 - 1)
+    return out
+
+
+def pattern_spec(n_items: int = 2_000, n_patterns: int = 500, mean_len: float = 10.0, per_row: int = 4,
+                 seed: int = 0, hash_seed: int = 777) -> PatternSpec:
+    """The deep sparse workload's tables: the same pattern pool, weights and length law as ``deep_sparse``."""
+    from math import exp, lgamma, log
+
+    rng = np.random.default_rng(seed)
+    plen = np.minimum(1 + rng.poisson(9, n_patterns), 16)
+    perm = rng.permutation(n_items)
+    wi = np.empty(n_items)
+    wi[perm] = zipf_weights(n_items, 1.0)
+    pats = _draw_without_replacement(rng, wi, plen)
+    pw = rng.exponential(1.0, n_patterns)
+    pat_cdf = np.cumsum(pw) / pw.sum()
+    # P(Poisson(mean) <= i) for i < 48: the length 1 + Poisson(mean) is capped at 49 (mass past it < 1e-12).
+    n_len = 48
+    pmf = np.array([exp(i * log(mean_len) - mean_len - lgamma(i + 1)) for i in range(n_len)])
+    len_cdf = np.minimum(np.cumsum(pmf), 1.0)
+    return PatternSpec(_u64_thresholds(len_cdf), _u64_thresholds(pat_cdf), pats.indptr.astype(np.int64),
+                       pats.items.astype(np.int32), int(_u64_thresholds(np.array([0.7]))[0]), n_items, per_row,
+                       hash_seed)
+
+
+def patterns_rows_host(spec: PatternSpec, n_rows: int, row0: int = 0) -> list[list[int]]:
+    """Rows ``row0 .. row0 + n_rows - 1`` of the hash-defined pattern workload, each in fill order (the host
+    restatement of ``etm_synth_patterns``; a Python loop per row, for small row counts)."""
+    seed = spec.hash_seed
+
+    def h(stream: int, r: int) -> int:
+        return int(bit_hash(seed, np.array([stream], np.uint64), np.array([r], np.uint64))[0])
+
+    out = []
+    for r in range(row0, row0 + n_rows):
+        hl = h(1, r)
+        length = 1 + sum(1 for t in spec.len_thr if hl >= int(t))
+        # The thresholds increase, so counting those reached equals scanning until the first one missed.
+        items: list[int] = []
+        for p in range(spec.per_row):
+            if len(items) >= length:
+                break
+            hp = h(2 + p, r)
+            j = 0
+            while j < len(spec.pat_thr) - 1 and hp >= int(spec.pat_thr[j]):
+                j += 1
+            for q in range(int(spec.pat_ptr[j]), int(spec.pat_ptr[j + 1])):
+                if len(items) >= length:
+                    break
+                if h(64 + 16 * p + (q - int(spec.pat_ptr[j])), r) >= spec.keep_thr:
+                    continue
+                x = int(spec.pat_items[q])
+                if x not in items:
+                    items.append(x)
+        t = 0
+        while len(items) < length and t < 65536:
+            x = h(4096 + t, r) % spec.n_items
+            t += 1
+            if x not in items:
+                items.append(x)
+        out.append(items)
+    return out
+
+
+def patterns_bitvecs_device(lib, spec: PatternSpec, n_rows: int, device="cuda"):
+    """Column bitvectors (torch uint64 [n_items, ceil(n_rows / 64)]) of the pattern workload, built on the
+    device by ``etm_synth_patterns``."""
+    import torch
+
+    ld = (n_rows + 63) // 64
+    t = {k: torch.from_numpy(v).to(device) for k, v in dict(
+        len_thr=spec.len_thr.view(np.int64), pat_thr=spec.pat_thr.view(np.int64), pat_ptr=spec.pat_ptr,
+        pat_items=spec.pat_items).items()}
+    bv = torch.empty((spec.n_items, ld), dtype=torch.int64, device=device)
+    st = lib.etm_synth_patterns(t["len_thr"].data_ptr(), len(spec.len_thr), t["pat_thr"].data_ptr(),
+                                len(spec.pat_thr), t["pat_ptr"].data_ptr(), t["pat_items"].data_ptr(), spec.per_row,
+                                spec.keep_thr, spec.n_items, n_rows, spec.hash_seed, bv.data_ptr(), ld,
+                                torch.cuda.current_stream().cuda_stream)
+    if st != 0:
+        raise RuntimeError(f"etm_synth_patterns failed: {lib.etm_last_error().decode()}")
+    return bv.view(torch.uint64)
+
+
 def _first_per_row(rid: np.ndarray, val: np.ndarray, n_items: int, lengths: np.ndarray):
     """Keep the first occurrence of each (row, item) in the given order, then the first ``lengths[r]`` per row."""
     _, first = np.unique(rid * n_items + val, return_index=True)

@@ -36,7 +36,9 @@ extern "C" {
 #define ETM_EINVAL 1   /* bad argument: sizes, alignment, widths */
 #define ETM_ECUDA 2    /* a CUDA call or launch failed */
 #define ETM_ENOSPACE 3 /* workspace or output capacity too small */
-#define ETM_ETIMEOUT 4 /* a bounded device wait gave up */
+#define ETM_ETIMEOUT 4 /* a bounded device wait gave up; the kernel cleaned up, the device stays usable */
+#define ETM_EUNSAFE 5  /* a bounded wait gave up and so did its cleanup wait: copies may still be landing;
+                          stop using the device (tear the process down) */
 
 /* Candidate classes written by etm_classify (gpu/kernels/_src/_subset_index.cu:27-33). */
 #define ETM_CAND_COUNT 0
@@ -51,16 +53,11 @@ extern "C" {
 #define ETM_METHOD_POPCOUNT 0 /* AND + popcount on CUDA cores */
 #define ETM_METHOD_TENSOR 1   /* 0/1 Gram on tcgen05 tensor cores, f32 accumulation in TMEM, exact */
 
-/* Flag added to etm_count_tiles_tc's elem: stage the A operand in tensor memory (tcgen05.st)
- * instead of shared memory. Exact either way; the shared-memory form is faster on GB300. */
-#define ETM_TC_A_TMEM 4
-/* Flag added to etm_count_tiles_tc's elem: the CTA-pair kernel (two SMs per 256 x 256 block pair,
- * tcgen05 cta_group::2); its work offsets count C(nb + 1, 2) block pairs per group (nb = ceil(m/256))
- * instead of nb (nb + 1) half tiles. */
-#define ETM_TC_PAIR 8
-/* Flag added to etm_count_tiles_tc's elem: the wide single-CTA kernel (one CTA per 256 x 256 block pair,
- * two M = 128 accumulators sharing each B tile); work offsets count C(nb + 1, 2) block pairs as for
- * ETM_TC_PAIR. */
+/* Element codes of etm_count_tiles_tc: 1 = e4m3 (kind::f8f6f4), 2 = f16 (kind::f16), ETM_TC_MXF4 = packed
+ * e2m1 under kind::mxf4 with unit block scales. Blocks hold etm_gram_block_members(elem) members: 256 for
+ * e4m3 and f16, 240 for e2m1. */
+#define ETM_TC_MXF4 4
+/* Accepted in elem for compatibility and ignored: every element code runs the block-pair kernel. */
 #define ETM_TC_WIDE 16
 
 /* Rows of one projection segment: 1024 bitvector words (65,536 transactions). */
@@ -107,6 +104,24 @@ int etm_gather_cols(const uint64_t* bv, int64_t ld, const int32_t* cols, int32_t
  */
 int etm_synth_bernoulli(const uint64_t* thresholds, int32_t n_items, int64_t n_rows, uint64_t seed,
                         uint64_t* out_bv, int64_t ld, void* stream);
+
+/*
+ * Bitvectors of a planted-pattern workload (the deep sparse configuration),
+ * defined by the same counter hash h(seed, stream, row) as
+ * etm_synth_bernoulli so a host restatement reproduces every bit. Row r: its
+ * length is 1 + #{i < n_len : h(seed, 1, r) >= len_thr[i]}; it draws per_row
+ * patterns, pattern p being the first j with h(seed, 2 + p, r) < pat_thr[j]
+ * (the last if none); item q of that pattern is kept when
+ * h(seed, 64 + 16 p + q, r) < keep_thr and not yet in the row, until the row
+ * is full; then noise items h(seed, 4096 + t, r) % n_items, t = 0, 1, ...,
+ * not yet in the row, fill it. Patterns: pat_ptr int64 [n_pat + 1] into
+ * pat_items int32 (at most 16 items each). out_bv uint64 [n_items][ld]
+ * (zeroed here). Test and benchmark input; no counterpart in the reference
+ * (its generator is synthetic.py:160-180, host only).
+ */
+int etm_synth_patterns(const uint64_t* len_thr, int32_t n_len, const uint64_t* pat_thr, int32_t n_pat,
+                       const int64_t* pat_ptr, const int32_t* pat_items, int32_t per_row, uint64_t keep_thr,
+                       int32_t n_items, int64_t n_rows, uint64_t seed, uint64_t* out_bv, int64_t ld, void* stream);
 
 /*
  * Prefix groups of a level. Replaces build_k3plus_groups_from_flat
@@ -240,19 +255,17 @@ int etm_count_tiles_proj(const uint64_t* cbuf, const int64_t* cbase, const int64
 
 /*
  * etm_count_tiles_proj on the tcgen05 tensor cores: the pair counts of each
- * listed group are the Gram matrix of its 0/1 member words, computed in work
- * items of 128 x 256 members (M = 128, N = 256) with bits expanded in shared
- * memory to f16 (elem 2, kind::f16) or e4m3 (elem 1, kind::f8f6f4) and f32
- * accumulation in TMEM. Exact while every group has at most 2^24 rows
- * (cwords <= 262144): the caller sends larger groups to the popcount kernels.
- * work_off counts work items: nb(nb+1) per group, nb = ceil(m/256) (the two
- * 128-member halves of super-tile ua against super-tile ub, ua <= ub; with
- * ETM_TC_WIDE or ETM_TC_PAIR the C(nb + 1, 2) block pairs ua <= ub);
- * n_tiles = work_off[n_work] (sizes the grid). work_counter (one int64 of
- * device memory, or NULL) lets the ETM_TC_WIDE kernel's CTAs claim items
- * dynamically (it is zeroed on the stream before the launch; concurrent calls
- * need separate counters); the other kernels take items round-robin. New in
- * this engine (the reference counts on CUDA cores only).
+ * listed group are the Gram matrix of its 0/1 member words. One persistent
+ * kernel takes block pairs (ua <= ub) of T = etm_gram_block_members(elem)
+ * members, stages the bits expanded to e4m3 (elem 1), f16 (elem 2) or packed
+ * e2m1 (ETM_TC_MXF4) in shared memory and accumulates in f32 in TMEM. Exact
+ * while every group has at most 2^24 rows (cwords <= 262144): the caller sends
+ * larger groups to the popcount kernels. work_off counts block pairs,
+ * C(nb + 1, 2) per group with nb = ceil(m / T); n_tiles = work_off[n_work]
+ * (sizes the grid). work_counter (one int64 of device memory, or NULL) lets
+ * the CTAs claim block pairs dynamically (zeroed on the stream before the
+ * launch; concurrent calls need separate counters). New in this engine (the
+ * reference counts on CUDA cores only).
  */
 int etm_count_tiles_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                        const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
@@ -260,11 +273,40 @@ int etm_count_tiles_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t
                        const uint8_t* cls, int32_t elem, int32_t* out_counts, int64_t* work_counter, void* stream);
 
 /*
+ * etm_count_tiles_tc with the survivor threshold fused into its epilogue, the
+ * form of count_shared_tiled_fused (gpu/kernels/_src/shared_tiled.cu:246-280):
+ * of the candidates it counts, only those reaching min_count get their count
+ * written (out_counts[t]) and their bit t set in surv_bits (uint32 words,
+ * bit t % 32 of word t / 32, chunk-relative t; the caller zeroes it first).
+ * The other slots of out_counts are left untouched.
+ */
+int etm_count_tiles_tc_sel(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
+                           const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
+                           const int64_t* work_off, int64_t n_work, int64_t n_tiles, int64_t chunk_base,
+                           const uint8_t* cls, int32_t elem, int32_t min_count, int32_t* out_counts,
+                           uint32_t* surv_bits, int64_t* work_counter, void* stream);
+
+/* Members per block of etm_count_tiles_tc for an element code (0 for an unknown code). */
+int etm_gram_block_members(int32_t elem);
+
+/*
  * Reads and clears the device status words the tensor-core kernels and the
  * projection (its bulk copies) raise when a bounded wait gives up
- * (synchronizes `stream`). Returns 0, or ETM_ETIMEOUT.
+ * (synchronizes `stream`). Returns 0, ETM_ETIMEOUT (the kernel gave up and
+ * cleaned up: its counts are incomplete, the device stays usable) or
+ * ETM_EUNSAFE (the projection's cleanup wait ran out too: stop using the
+ * device). The words are per device, shared by every caller of the library.
  */
 int etm_device_status(void* stream);
+
+/*
+ * Limits of the first bounded waits, in nanoseconds: the Gram's MMA thread
+ * waiting for a filled stage and the projection waiting for a group's bulk
+ * copies (negative: the default of 2 s; 0: give up at once, which drives the
+ * give-up path without a real stall). The cleanup waits keep their own 2 s
+ * limit. Applies to launches after the call, process-wide.
+ */
+int etm_set_wait_limits(int64_t gram_first_wait_ns, int64_t proj_first_wait_ns);
 
 /*
  * Survivors of a counted chunk (groups [g0, g1)), in candidate order, decoded

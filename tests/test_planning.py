@@ -34,14 +34,13 @@ def test_projected_stride_bounds_the_segmented_layout(engm, n_words):
 
 
 def test_gram_items_per_kernel_form(engm):
-    m = np.array([1, 2, 256, 257, 512, 1255])
-    nb = (m + 255) // 256
-    assert np.array_equal(engm._tile_items(m, 1, 1), nb * (nb + 1))  # 128 x 256 items
-    for flag in (engm.TC_PAIR, engm.TC_WIDE):
-        assert np.array_equal(engm._tile_items(m, 1, 1 | flag), nb * (nb + 1) // 2)  # block pairs
+    m = np.array([1, 2, 240, 241, 256, 257, 512, 1255])
+    for elem, t in ((1, 256), (2, 256), (1 | engm.TC_WIDE, 256), (engm.TC_MXF4, 240)):
+        nb = (m + t - 1) // t
+        assert engm.tc_block(elem) == t
+        assert np.array_equal(engm._tile_items(m, 1, elem), nb * (nb + 1) // 2)  # block pairs ua <= ub
     nt = (m + 63) // 64
     assert np.array_equal(engm._tile_items(m, 0), nt * (nt + 1) // 2)  # popcount tile-pairs
-    assert engm.DEFAULT_TC_ELEM & engm.TC_WIDE
 
 
 def test_row_wise_crossovers_are_the_reference_constants(engm):
