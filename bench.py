@@ -408,6 +408,9 @@ def _pkg():
     return g.package()
 
 
+#: Operand formats of the tensor-core Gram by element code.
+OPERANDS = {1: "e4m3 (kind::f8f6f4)", 2: "f16 (kind::f16)", 4: "packed e2m1 (kind::mxf4, unit block scales)"}
+
 METRIC = "mine() seconds, dense K=2 stress (2M x 4096, s=0.002, max_length=3), exact counts, batched form"
 
 
@@ -422,8 +425,9 @@ def main() -> None:
     ap.add_argument("--serving-scale", type=float, default=1.0, help="serving: dataset row scale")
     ap.add_argument("--serving-requests", type=int, default=256)
     ap.add_argument("--method", default=None, choices=["popcount", "tensor"])
-    ap.add_argument("--tc-elem", type=int, default=17, choices=[1, 2, 9, 10, 17, 18],
-                    help="tensor operands: 1 = e4m3, 2 = f16; + 8: the CTA-pair kernel; + 16: the 256 x 256 kernel")
+    ap.add_argument("--tc-elem", type=int, default=None, choices=[1, 2, 4, 17, 18, 20],
+                    help="tensor operands: 1 = e4m3, 2 = f16, 4 = packed e2m1 (kind::mxf4); + 16 is ignored "
+                         "(default: the engine's)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparator")
     ap.add_argument("--proj-gb", type=float, default=8.0, help="device GB of projected words per chunk")
     ap.add_argument("--chunk-cands", type=int, default=None, help="candidates per chunk (default: the engine's)")
@@ -467,6 +471,8 @@ def main() -> None:
 
     engm = import_module(pkg.__name__ + ".engine")
     method = args.method or engm.DEFAULT_METHOD
+    if args.tc_elem is None:
+        args.tc_elem = engm.DEFAULT_TC_ELEM
     bv = dense_k2_device(pkg, lib, spec)
     n_rows = spec["n_rows"]
     extra = {"chunk_cands": args.chunk_cands} if args.chunk_cands else {}
@@ -508,7 +514,8 @@ def main() -> None:
     # Plain form (one counting launch per prefix group): the comparator.
     plain = None
     if not args.no_plain:
-        pe = engm.Engine(form="plain", method=method, tc_elem=args.tc_elem, proj_bytes=int(args.proj_gb * (1 << 30)))
+        pe = engm.Engine(form="plain", method=method, tc_elem=args.tc_elem, proj_bytes=int(args.proj_gb * (1 << 30)),
+                         **extra)
         one(pe)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -548,13 +555,21 @@ def main() -> None:
         top = max(kern.values(), key=lambda r: r["ms"])
         per_launch_s = top["ms"] / top["launches"] / 1e3
         if top["name"] == "gram_tc":
-            # Useful work: 2 x C(m,2) x rows per group; the e4m3 MMAs run at twice the dense bf16 rate.
-            fp8 = method == "tensor" and eng.tc_elem & 3 == 1
-            peak = peaks["bf16_tflops"] * (2.0 if fp8 else 1.0)
+            # Useful work: 2 x C(m,2) x rows per group, against the measured dense rate of the Gram's own MMA
+            # shape and operand format (etm_tc_mma_rate: back-to-back MMAs on every SM, CUDA events).
+            import ctypes
+
+            rate = ctypes.c_double(0.0)
+            st = lib.etm_tc_mma_rate(eng.tc_elem, 20000, ctypes.byref(rate), torch.cuda.current_stream().cuda_stream)
+            if st != 0:
+                raise RuntimeError(lib.etm_last_error().decode())
+            peak = rate.value
             achieved = top["flops"] / top["launches"] / per_launch_s / 1e12
             roof = {"bound": "tensor", "kernel": top["name"], "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                     "frac": achieved / peak,
-                    "peak_source": f"{peaks['source']} bf16 dense" + (" x 2 (e4m3 operands)" if fp8 else ""),
+                    "peak_source": f"measured: etm_tc_mma_rate({eng.tc_elem}) = {OPERANDS[eng.tc_elem & 7]} MMAs of "
+                                   "the Gram's shape back to back on every SM (bf16 cuBLAS burst in "
+                                   f"MEASURED_PEAKS.json: {peaks['bf16_tflops']:.0f})",
                     "work": "2 * C(m,2) * rows per prefix group (upper-triangle pair counts)"}
         else:
             achieved = top["bytes"] / top["launches"] / per_launch_s / 1e9
@@ -597,9 +612,8 @@ def main() -> None:
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (hash-defined Bernoulli bits, on device)",
             "config": {"workload": args.workload, **spec, "method": method, "form": "batched",
-                       "tc_operands": (("e4m3" if args.tc_elem & 3 == 1 else "f16")
-                                       + (", CTA pairs (cta_group::2)" if args.tc_elem & 8 else "")
-                                       + (", 256 x 256 tiles" if args.tc_elem & 16 else ", 128 x 256 tiles"))
+                       "tc_operands": (f"{OPERANDS[args.tc_elem & 7]}, {engm.tc_block(args.tc_elem)} x "
+                                       f"{engm.tc_block(args.tc_elem)} block pairs")
                        if method == "tensor" else None,
                        "l2": "inputs (1.02 GB of bitvectors) larger than L2; no flush",
                        "parallelism": "replicas" if world > 1 else "1 GPU"},

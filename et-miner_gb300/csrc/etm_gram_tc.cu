@@ -485,6 +485,70 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
     if (tid == 0 && *abort_flag) atomicExch(&g_tc_status, ETM_ETIMEOUT);
 }
 
+// Issue rate of the Gram's own MMA shape: one CTA per SM, one thread issuing `iters` back-to-back MMAs
+// (M = 128, N = T, the format's K per instruction) on a zeroed shared-memory tile into one accumulator,
+// then a bounded wait for their completion. The roofline's tensor peak for that operand format.
+template <int FMT>
+__global__ void __launch_bounds__(128, 1) mma_rate_kernel(int64_t iters, int* status) {
+    extern __shared__ uint8_t dsmem[];
+    __shared__ __align__(8) uint64_t done_bar;
+    __shared__ uint32_t tmem_sh;
+    uint8_t* tiles = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < 3 * HALF_BYTES / 16; i += blockDim.x) reinterpret_cast<uint4*>(tiles)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        mbar_init(&done_bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_proxy_async();
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_sh)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        tc_fence_before();
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_sh;
+    if constexpr (FMT == 4) {
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + SF_COL;
+        const uint32_t u = 0x7F7F7F7Fu;
+        asm volatile(
+            "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,"
+            "%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr),
+            "r"(u)
+            : "memory");
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    }
+    if (tid == 0) {
+        const uint32_t a = smem_u32(tiles), b = a + HALF_BYTES;
+        for (int64_t it = 0; it < iters; it++) {
+            const int k = (int)(it & 3);
+            mma_ss<FMT>(tmem, smem_desc(a + 32 * k), smem_desc(b + 32 * k), it > 0 ? 1u : 0u, tmem + SF_COL);
+        }
+        mma_commit(&done_bar);
+        const uint64_t t0 = now_ns();
+        bool ok = true;
+        while (!mbar_test(&done_bar, 0)) {
+            if (now_ns() - t0 > WAIT_NS) {
+                ok = false;
+                break;
+            }
+            __nanosleep(128);
+        }
+        if (!ok) atomicExch(status, ETM_ETIMEOUT);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
 std::mutex g_cfg_lock;
 // The MMA thread's wait for a filled stage: WAIT_NS unless a test set it (0 = give up at once).
 uint64_t g_first_wait_ns = WAIT_NS;
@@ -573,6 +637,58 @@ extern "C" int etm_count_tiles_tc_sel(const uint64_t* cbuf, const int64_t* cbase
 }
 
 extern "C" int etm_gram_block_members(int32_t elem) { return etm::gram_block_members(elem); }
+
+namespace {
+template <int FMT>
+int mma_rate(int64_t iters, int* status, cudaStream_t s) {
+    constexpr int smem = 3 * HALF_BYTES + 1024;
+    ETM_CUDA(cudaFuncSetAttribute(mma_rate_kernel<FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    mma_rate_kernel<FMT><<<max(1, sm_count()), 128, smem, s>>>(iters, status);
+    ETM_LAUNCHED("mma_rate");
+    return ETM_OK;
+}
+}  // namespace
+
+extern "C" int etm_tc_mma_rate(int32_t elem, int64_t iters, double* out_tflops, void* stream) {
+    // Times `iters` MMAs per SM of the Gram's shape for `elem` on every SM (CUDA events on `stream`, which is
+    // synchronized) and returns the dense rate in TFLOP/s: 2 M N K per MMA.
+    const int e = elem & ~ETM_TC_WIDE;
+    ETM_REQUIRE(e == 1 || e == 2 || e == ETM_TC_MXF4, ETM_EINVAL, "etm_tc_mma_rate: element code %d", elem);
+    ETM_REQUIRE(iters > 0 && iters < (1LL << 32) && out_tflops != nullptr, ETM_EINVAL, "etm_tc_mma_rate: bad iters");
+    cudaStream_t s = as_stream(stream);
+    int* status = nullptr;
+    ETM_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&status), g_tc_status));
+    cudaEvent_t e0, e1;
+    ETM_CUDA(cudaEventCreate(&e0));
+    ETM_CUDA(cudaEventCreate(&e1));
+    int st = ETM_OK;
+    auto run = [&]() { return e == ETM_TC_MXF4 ? mma_rate<4>(iters, status, s) : e == 2 ? mma_rate<2>(iters, status, s)
+                                                                                         : mma_rate<1>(iters, status, s); };
+    st = run();  // warm-up
+    if (st == ETM_OK) {
+        cudaEventRecord(e0, s);
+        st = run();
+        cudaEventRecord(e1, s);
+    }
+    float ms = 0.f;
+    if (st == ETM_OK) {
+        const cudaError_t err = cudaEventSynchronize(e1);
+        if (err != cudaSuccess) {
+            etm::set_error("etm_tc_mma_rate: %s", cudaGetErrorString(err));
+            st = ETM_ECUDA;
+        } else {
+            cudaEventElapsedTime(&ms, e0, e1);
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != ETM_OK) return st;
+    const double k = e == ETM_TC_MXF4 ? 64.0 : e == 1 ? 32.0 : 16.0;
+    const double n = e == ETM_TC_MXF4 ? Fmt<4>::T : Fmt<1>::T;
+    const double flops = 2.0 * 128.0 * n * k * (double)iters * (double)max(1, sm_count());
+    *out_tflops = ms > 0.f ? flops / (ms * 1e-3) / 1e12 : 0.0;
+    return ETM_OK;
+}
 
 extern "C" int etm_set_wait_limits(int64_t gram_first_wait_ns, int64_t proj_first_wait_ns) {
     {

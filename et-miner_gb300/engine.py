@@ -83,8 +83,9 @@ def proj_stride(pcnt: np.ndarray, n_words: int) -> np.ndarray:
 
 TC_MXF4 = 4  # ETM_TC_MXF4: packed e2m1 operands under kind::mxf4 (tc_elem code)
 TC_WIDE = 16  # ETM_TC_WIDE: accepted in tc_elem and ignored (every code runs the block-pair kernel)
-#: e4m3 operands: the fastest exact form measured on GB300.
-DEFAULT_TC_ELEM = 1 | TC_WIDE
+#: Packed e2m1 operands: the fastest exact form measured on GB300 (0.86 s per dense K=2 mine against 1.11 s
+#: with e4m3 operands).
+DEFAULT_TC_ELEM = TC_MXF4
 
 
 def tc_block(tc_elem: int = DEFAULT_TC_ELEM) -> int:

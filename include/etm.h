@@ -290,6 +290,15 @@ int etm_count_tiles_tc_sel(const uint64_t* cbuf, const int64_t* cbase, const int
 int etm_gram_block_members(int32_t elem);
 
 /*
+ * Dense tensor-core rate of the Gram's MMA shape for `elem` (M = 128, N = the
+ * block size, the format's K per instruction), in TFLOP/s: every SM issues
+ * `iters` back-to-back MMAs on a zeroed shared-memory tile, timed with CUDA
+ * events on `stream` (synchronized). The roofline's tensor peak for that
+ * operand format. No counterpart in the reference.
+ */
+int etm_tc_mma_rate(int32_t elem, int64_t iters, double* out_tflops, void* stream);
+
+/*
  * Reads and clears the device status words the tensor-core kernels and the
  * projection (its bulk copies) raise when a bounded wait gives up
  * (synchronizes `stream`). Returns 0, ETM_ETIMEOUT (the kernel gave up and
