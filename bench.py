@@ -10,15 +10,24 @@ between steps.
 
 Prints ONE JSON line (rank 0):
   value         seconds per mine, batched form (device-resident input)
+  exact         the benchmarked result checked: sampled recounts in plain
+                PyTorch, subset closure, completeness/absence of random
+                extensions, level 1 complete (verify.check_mine)
   plain         the one-launch-per-prefix-group form on the same input
   e2e           seconds per mine through apriori(bitvecs=...) with the
                 bitvectors copied from pinned host memory and the itemsets
                 copied back inside the timed region
-  roofline      the dominant counting kernel: algorithmic bytes per launch over
-                its CUDA-event time, against the measured HBM copy peak
-  cpu_baseline  the CPU oracle on a bounded sample, extrapolated per row
-``--impl reference`` times the CPU restatement of the reference's counting
-path (the oracle) on the host cores instead, on the same workload.
+  roofline      the dominant kernel: useful work per launch over its
+                CUDA-event time, against the measured peak of its unit (the
+                Gram's own MMA rate for the tensor-core kernel)
+  cpu_baseline  the reference's CPU route (oracle/cpu_route.py) on every host
+                core, on the same input, under a time budget: measured, a
+                lower bound when the budget ran out before the mine finished
+  workloads     the plain small workload through the transactions route and
+                the deep sparse workload (20M rows, generator pruning), each
+                with its own check and CPU route beside it
+``--impl reference`` runs the reference's CPU route alone on the same
+workload, each step one budgeted mine.
 
 Multi-GPU: the path does not shard in this engine (replicas only); under
 torchrun every rank mines its own copy and the max over ranks is reported.
@@ -135,90 +144,83 @@ LEVEL_CANDIDATES = {
 }
 
 
-_MP_BV = None
+_MP_SPEC = None
 
 
-def _mp_init(bv) -> None:
-    global _MP_BV
-    _MP_BV = bv
+def _mp_init(spec) -> None:
+    global _MP_SPEC
+    _MP_SPEC = spec
 
 
-def _mp_count(sets) -> int:
-    from oracle import miner
+def _mp_item_rows(items) -> list:
+    """Row ids holding each listed item of the hash-defined Bernoulli workload (host restatement of
+    etm_synth_bernoulli), in chunks of 2^20 rows."""
+    import __graft_entry__ as g
 
-    miner.count_itemsets(sets, _MP_BV)
-    return len(sets)
+    syn = g.package().synthetic
+    thr, n_rows, seed = _MP_SPEC
+    out = []
+    for i in items:
+        parts = []
+        for r0 in range(0, n_rows, 1 << 20):
+            rows = np.arange(r0, min(n_rows, r0 + (1 << 20)), dtype=np.uint64)
+            h = syn.bit_hash(seed, np.full(len(rows), i, dtype=np.uint64), rows)
+            parts.append(np.flatnonzero(h < thr[i]).astype(np.int32) + r0)
+        out.append(np.concatenate(parts))
+    return out
 
 
-def cpu_estimate(spec, level_cands, budget_s: float = 12.0, bv_host=None, workers: int = 1) -> dict:
-    """Seconds the CPU oracle's counting would take on the whole workload, from a timed sample.
+def dense_k2_host_csr(pkg, spec, workers: int):
+    """The dense K=2 workload as the CPU route's input: the frequent-column CSR of the transactions (built on
+    the host cores from the same hash-defined bits the device generates), and the seconds it took."""
+    import multiprocessing as mp
 
-    The oracle counts a candidate by ANDing its k column bitvectors and
-    popcounting (count_per_candidate, core/cpu_miner.py:794-809), a cost
-    that depends on k and the words per column, not on the bits. Per level
-    a sample of candidates over full-length columns (the workload's own when
-    ``bv_host`` is given, else random words of the same length) is timed and
-    scaled by the level's candidate count; K=1 is one popcount per column.
-    With ``workers`` > 1 the sample is split over that many spawned processes
-    and the wall time of the whole sample is what is scaled.
-    """
-    from oracle import miner
+    from oracle import cpu_route
 
-    n_words = (spec["n_rows"] + 63) // 64
-    rng = np.random.default_rng(1)
-    if bv_host is None:
-        n_s = 128
-        bv = rng.integers(0, 2**63, size=(n_s, n_words), dtype=np.int64).view(np.uint64)
-    else:
-        n_s = min(128, bv_host.shape[0])
-        bv = np.ascontiguousarray(bv_host[:n_s])
-    pool = None
-    if workers > 1:
-        import multiprocessing as mp
+    t0 = time.perf_counter()
+    syn = pkg.synthetic
+    thr = syn.bernoulli_thresholds(syn.dense_k2_probs(spec["n_items"], seed=spec["seed"]))
+    items = np.array_split(np.arange(spec["n_items"]), max(1, 4 * workers))
+    with mp.get_context("spawn").Pool(workers, initializer=_mp_init,
+                                      initargs=((thr, spec["n_rows"], spec["hash_seed"]),)) as pool:
+        rows = [r for part in pool.map(_mp_item_rows, items, chunksize=1) for r in part]
+    indptr, cols = cpu_route.csr_from_column_rows(rows, spec["n_rows"])
+    del rows
+    fp, fc, kept = cpu_route.frequent_csr(indptr, cols, spec["n_items"], spec["n_rows"], spec["min_support"])
+    return (fp, fc, len(kept)), time.perf_counter() - t0
 
-        pool = mp.get_context("spawn").Pool(workers, initializer=_mp_init, initargs=(bv,))
-        pool.map(_mp_count, [np.zeros((1, 2), np.int32)] * workers, chunksize=1)  # workers up and importing done
 
-    def timed(sets: np.ndarray) -> float:
-        if pool is None:
-            t0 = time.perf_counter()
-            miner.count_itemsets(sets, bv)
-            return time.perf_counter() - t0
-        parts = np.array_split(sets, workers)
-        t0 = time.perf_counter()
-        pool.map(_mp_count, parts, chunksize=1)
-        return time.perf_counter() - t0
+def cpu_route_timed(csr, n_rows: int, min_support: float, max_length, budget_s: float | None, workers: int,
+                    **flags) -> dict:
+    """One mine of the reference's CPU route (oracle/cpu_route.py) on the host cores: measured seconds, and
+    whether it finished within ``budget_s`` (if not, the seconds are a lower bound of the whole mine's)."""
+    from oracle import cpu_route
 
-    per_level = []
-    total = 0.0
-    t_k1 = time.perf_counter()
-    miner.popcount_rows(bv)
-    t_k1 = (time.perf_counter() - t_k1) / n_s
-    total += t_k1 * level_cands[0]
-    per_level.append({"k": 1, "candidates": level_cands[0], "s_per_candidate": t_k1})
-    cap = 65536 * max(1, workers)
+    indptr, cols, n_cols = csr
+    r = cpu_route.mine(indptr, cols, n_cols, n_rows, min_support, max_length, workers=workers, budget_s=budget_s,
+                       **flags)
+    return {"value": r.seconds, "complete": r.complete, "counted": r.counted, "itemsets": sum(len(s) for s, _ in r.levels),
+            "levels": r.levels}
+
+
+def cpu_model() -> str:
     try:
-        for k, n_c in enumerate(level_cands[1:], start=2):
-            sample = 256
-            while True:
-                sets = np.sort(np.stack([rng.choice(n_s, size=k, replace=False) for _ in range(sample)]), axis=1)
-                dt = timed(sets.astype(np.int32))
-                if dt > budget_s / (2 * len(level_cands)) or sample >= cap:
-                    break
-                sample *= 4
-            per = dt / sample
-            total += per * n_c
-            per_level.append({"k": k, "candidates": n_c, "s_per_candidate": per, "sampled": sample})
-    finally:
-        if pool is not None:
-            pool.close()
-            pool.join()
-    return {"value": total, "unit": "s", "cores": max(1, workers), "kind": "port",
-            "sample": "oracle/miner.py count_itemsets (AND + popcount per candidate, core/cpu_miner.py:794-809) "
-                      f"timed on sampled candidates over {n_words:,}-word columns"
-                      + (f", split over {workers} processes," if workers > 1 else ",")
-                      + " scaled by each level's candidate count",
-            "levels": per_level}
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu part", "hardware")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
+def _baseline_entry(run: dict, cores: int, what: str) -> dict:
+    return {"value": run["value"], "unit": "s", "cores": cores, "kind": "port",
+            "lower_bound": not run["complete"], "counted": run["counted"], "cpu": cpu_model(),
+            "sample": what + (" (the whole mine)" if run["complete"] else
+                              " until the time budget ran out: the value is the measured time of the part counted "
+                              "(see counted), a lower bound of the whole mine's time, not an extrapolation")}
 
 
 def max_over_ranks(value: float, dist=None, device: str = "cuda") -> float:
@@ -233,20 +235,30 @@ def max_over_ranks(value: float, dist=None, device: str = "cuda") -> float:
     return float(t.item())
 
 
+ROUTE_SAMPLE = ("oracle/cpu_route.py mine: the reference's CPU route (scipy Gram column blocks for K=2, prefix-group "
+                "projection Grams for K>=3, core/cpu_miner.py:332-378, 727-791, 1066-1161) over a thread pool of "
+                "every host core")
+
+
 def run_reference(args, spec) -> None:
-    cands = LEVEL_CANDIDATES.get(args.workload)
-    if cands is None:
-        print(json.dumps({"impl": "reference", "unavailable": f"no recorded candidate counts for {args.workload}"}))
-        return
-    base = cpu_estimate(spec, cands, budget_s=max(6.0, 30.0 / max(1, args.steps + args.warmup)),
-                        workers=max(1, os.cpu_count() or 1))
+    """The reference's CPU route on the same workload, on every host core: each timed step one mine under a
+    time budget (the whole run stays within a few minutes)."""
+    pkg = _pkg()
+    workers = max(1, os.cpu_count() or 1)
+    csr, build_s = dense_k2_host_csr(pkg, spec, workers)
+    budget = args.ref_budget if args.ref_budget else max(20.0, min(90.0, 180.0 / max(1, args.steps)))
+    runs = [cpu_route_timed(csr, spec["n_rows"], spec["min_support"], spec["max_length"], budget, workers)
+            for _ in range(max(1, args.steps))]
+    value = statistics.median(r["value"] for r in runs)
+    base = _baseline_entry(runs[0], workers, ROUTE_SAMPLE + f", {budget:.0f} s budget per step")
+    base["value"] = value
     line = {
-        "impl": "reference", "metric": METRIC, "value": base["value"], "unit": "s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["value"] * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": args.workload, **spec},
-        "cpu_baseline": base,
-        "e2e": {"value": base["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
+        "steps": len(runs), "warmup": 0, "ms_per_step": value * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (hash-defined Bernoulli bits, host)",
+        "config": {"workload": args.workload, **spec}, "lower_bound": not runs[0]["complete"],
+        "input_build_s": build_s, "cpu_baseline": base,
+        "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -258,37 +270,29 @@ TX_WORKLOADS = {
 }
 
 
-def run_transactions(args) -> None:
-    """The transactions route on the plain small workload (60K rows x 1,000 Zipf(1.1) items, s=0.01):
-    seconds per ``apriori(transactions, use_gpu=True)`` call (transaction CSR on the host in, result frame
-    out), the kernels it ran, exactness against the CPU oracle, and the oracle's whole mine of the same
-    input timed beside it (this workload is small enough for the oracle to run in full)."""
+def _tx_cpu_mine(t, spec):
+    """The CPU route of a transactions workload on every host core: the frequent-item CSR, then the level
+    loop (both timed): (seconds, canonical result, cores)."""
+    from oracle import cpu_route, miner
+
+    workers = max(1, os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    csr = miner.transaction_csr(t.indptr, t.items, t.n_rows, spec["min_support"])
+    r = cpu_route.mine(csr.indptr, csr.cols, csr.n_cols, t.n_rows, spec["min_support"], spec["max_length"],
+                       workers=workers)
+    return time.perf_counter() - t0, miner.canonical(r.levels, csr.items), workers
+
+
+def transactions_line(pkg, name: str, steps: int, warmup: int, with_cpu: bool = True) -> dict:
+    """The transactions route on a workload of TX_WORKLOADS (the plain small one: 60K rows x 1,000
+    Zipf(1.1) items, s=0.01): seconds per ``apriori(transactions, use_gpu=True)`` call (transaction CSR on the
+    host in, result frame out), the kernels it ran, exactness against the CPU route's own result, and the CPU
+    route's whole mine of the same input timed beside it (small enough to run in full)."""
     import torch
 
-    from oracle import miner
-
-    spec = TX_WORKLOADS[args.workload]
-    pkg = _pkg()
-    syn = pkg.synthetic
-    t = getattr(syn, spec["gen"])(seed=spec["seed"])
+    spec = TX_WORKLOADS[name]
+    t = getattr(pkg.synthetic, spec["gen"])(seed=spec["seed"])
     n_rows = t.n_rows
-
-    def cpu_mine():
-        t0 = time.perf_counter()
-        res, col_items = miner.mine_transactions(t.indptr, t.items, n_rows, spec["min_support"], spec["max_length"])
-        return time.perf_counter() - t0, miner.canonical(res.levels, col_items)
-
-    if args.impl == "reference":
-        cpu_s, _ = cpu_mine()
-        base = {"value": cpu_s, "unit": "s", "cores": 1, "kind": "port",
-                "sample": "oracle/miner.py mine_transactions: the whole mine of the workload, one core"}
-        print(json.dumps({"impl": "reference", "metric": TX_METRIC, "value": cpu_s, "unit": "s", "n_gpus": args.gpus,
-                          "steps": 1, "warmup": 0, "ms_per_step": cpu_s * 1e3, "higher_is_better": False,
-                          "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-                          "config": {"workload": args.workload, **spec}, "cpu_baseline": base,
-                          "e2e": {"value": cpu_s, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
-              flush=True)
-        return
     pkg.build_library()
     from importlib import import_module
 
@@ -304,37 +308,145 @@ def run_transactions(args) -> None:
                            level_callback=lambda k, nc, nf, ms: levels.append({"k": k, "candidates": nc,
                                                                                "frequent": nf}))
 
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, warmup)):
         df = call()
     torch.cuda.synchronize()
     eng.reset_kernel_times()
     launches0 = eng.launches
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         df = call()
     torch.cuda.synchronize()
-    dt = (time.perf_counter() - t0) / args.steps
+    dt = (time.perf_counter() - t0) / steps
     clk = clocks.stop()
     kern = eng.kernel_report()
-    cpu_s, want = cpu_mine()
     got = pkg.result_pairs(df, n_rows)
     n_sets = len(got)
     n_vals = sum(len(s) for s, _ in got)
     line = {
-        "metric": TX_METRIC, "value": dt, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "metric": TX_METRIC, "value": dt, "unit": "s", "n_gpus": 1, "steps": steps, "warmup": warmup,
         "ms_per_step": dt * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (seeded plain_small generator, host CSR)",
-        "config": {"workload": args.workload, **spec, "route": "transactions"},
-        "levels": list(levels), "exact": got == want, "itemsets": n_sets,
+        "config": {"workload": name, **spec, "route": "transactions"},
+        "levels": list(levels), "itemsets": n_sets,
         "e2e": {"value": dt, "unit": "s", "h2d_bytes_per_step": int(t.indptr.nbytes + t.items.nbytes),
                 "d2h_bytes_per_step": 8 * n_vals + 16 * n_sets + 8},
-        "kernels": kern, "gpu_launches": (eng.launches - launches0) // args.steps,
-        "cpu_baseline": {"value": cpu_s, "unit": "s", "cores": 1, "kind": "port",
-                         "sample": "oracle/miner.py mine_transactions: the whole mine of the workload, one core"},
-        "clocks": clk,
+        "kernels": kern, "gpu_launches": (eng.launches - launches0) // steps, "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    if with_cpu:
+        cpu_s, want, workers = _tx_cpu_mine(t, spec)
+        line["exact"] = got == want
+        line["cpu_baseline"] = {"value": cpu_s, "unit": "s", "cores": workers, "kind": "port", "lower_bound": False,
+                                "cpu": cpu_model(),
+                                "sample": "oracle/miner.py transaction_csr + " + ROUTE_SAMPLE + " (the whole mine)"}
+    return line
+
+
+def run_transactions(args) -> None:
+    spec = TX_WORKLOADS[args.workload]
+    pkg = _pkg()
+    if args.impl == "reference":
+        t = getattr(pkg.synthetic, spec["gen"])(seed=spec["seed"])
+        cpu_s, _, workers = _tx_cpu_mine(t, spec)
+        base = {"value": cpu_s, "unit": "s", "cores": workers, "kind": "port", "lower_bound": False,
+                "cpu": cpu_model(), "sample": "oracle/miner.py transaction_csr + " + ROUTE_SAMPLE + " (the whole mine)"}
+        print(json.dumps({"impl": "reference", "metric": TX_METRIC, "value": cpu_s, "unit": "s", "n_gpus": args.gpus,
+                          "steps": 1, "warmup": 0, "ms_per_step": cpu_s * 1e3, "higher_is_better": False,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+                          "config": {"workload": args.workload, **spec}, "cpu_baseline": base,
+                          "e2e": {"value": cpu_s, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+              flush=True)
+        return
+    print(json.dumps(transactions_line(pkg, args.workload, args.steps, args.warmup)), flush=True)
+
+
+#: The deep sparse workload: 20M transactions over 2,000 items from 500 planted patterns (hash-defined,
+#: generated on the device), min_support 0.005, max_length 16, generator pruning.
+DEEP_SPARSE = dict(n_rows=20_000_000, n_items=2_000, min_support=0.005, max_length=16, use_generator_pruning=True,
+                   pattern_seed=0, hash_seed=777)
+
+
+def device_bitvecs_to_host_csr(bv, n_rows: int, chunk_cols: int = 64):
+    """The row-major CSR (indptr int64, column ids int32) of device bitvectors, built on the device (bits
+    unpacked per column chunk, entries sorted by row) and copied to the host: the CPU route's input."""
+    import torch
+
+    n_cols = bv.shape[0]
+    b = bv.view(torch.int64)
+    shifts = torch.arange(64, device=b.device, dtype=torch.int64)
+    keys = []
+    for c0 in range(0, n_cols, chunk_cols):
+        x = b[c0:c0 + chunk_cols]
+        bits = ((x[:, :, None] >> shifts) & 1).view(x.shape[0], -1)[:, :n_rows]
+        col, row = torch.nonzero(bits, as_tuple=True)
+        keys.append(row * n_cols + (col + c0))
+        del bits
+    k = torch.sort(torch.cat(keys)).values
+    rows, cols = k // n_cols, (k % n_cols).to(torch.int32)
+    indptr = torch.zeros(n_rows + 1, dtype=torch.int64, device=b.device)
+    indptr[1:] = torch.cumsum(torch.bincount(rows, minlength=n_rows), 0)
+    return indptr.cpu().numpy(), cols.cpu().numpy()
+
+
+def deep_sparse_line(pkg, lib, steps: int, warmup: int, with_cpu: bool, cpu_budget_s: float = 40.0) -> dict:
+    """The deep sparse workload mined on the device (bitvectors resident), checked by ``verify.check_mine``,
+    with the CPU route on the same input under a time budget beside it."""
+    import torch
+    from importlib import import_module
+
+    engm = import_module(pkg.__name__ + ".engine")
+    verm = import_module(pkg.__name__ + ".verify")
+    spec = DEEP_SPARSE
+    syn = pkg.synthetic
+    n_rows = spec["n_rows"]
+    ps = syn.pattern_spec(n_items=spec["n_items"], seed=spec["pattern_seed"], hash_seed=spec["hash_seed"])
+    bv = syn.patterns_bitvecs_device(lib, ps, n_rows)
+    eng = engm.Engine()
+
+    def one():
+        return eng.mine(bv, n_rows, spec["min_support"], spec["max_length"], use_generator_pruning=True)
+
+    for _ in range(max(1, warmup)):
+        out = one()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = eng.launches
+    start.record()
+    for _ in range(steps):
+        out = one()
+    end.record()
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end) / steps
+    rep = verm.check_mine(out, bv, n_rows, generators=True, max_length=spec["max_length"], sample=10_000)
+    line = {"workload": "deep_sparse", "config": {**spec, "rows_generated_on": "device (etm_synth_patterns)"},
+            "metric": "mine() seconds, bitvectors resident", "value": ms / 1e3, "unit": "s", "steps": steps,
+            "levels": [{"k": s.k, "candidates": s.n_candidates, "frequent": s.n_frequent} for s in out.stats],
+            "itemsets": out.n_itemsets(), "gpu_launches": (eng.launches - launches0) // steps,
+            "exact": {"sampled": rep["sampled"], "mismatches": rep["mismatches"],
+                      "extensions_checked": rep["extensions_checked"], "level1_complete": rep["level1_complete"]}}
+    if with_cpu:
+        t0 = time.perf_counter()
+        indptr, cols = device_bitvecs_to_host_csr(bv, n_rows)
+        from oracle import cpu_route
+
+        csr = cpu_route.frequent_csr(indptr, cols, spec["n_items"], n_rows, spec["min_support"])
+        build_s = time.perf_counter() - t0
+        workers = max(1, os.cpu_count() or 1)
+        run = cpu_route_timed((csr[0], csr[1], len(csr[2])), n_rows, spec["min_support"], spec["max_length"],
+                              cpu_budget_s, workers, use_generator_pruning=True)
+        line["cpu_baseline"] = _baseline_entry(run, workers, ROUTE_SAMPLE + f", {cpu_budget_s:.0f} s budget")
+        line["cpu_baseline"]["input_build_s"] = build_s
+        if run["complete"]:
+            from oracle import miner
+
+            got = [(c, n) for c, n in out.host_levels()]
+            line["cpu_baseline"]["equal_to_engine"] = miner.canonical(got) == miner.canonical(
+                [(csr[2][s], c) for s, c in run["levels"]])
+        del run
+    del bv
+    torch.cuda.empty_cache()
+    return line
 
 
 def run_serving(args) -> None:
@@ -431,7 +543,11 @@ def main() -> None:
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparator")
     ap.add_argument("--proj-gb", type=float, default=8.0, help="device GB of projected words per chunk")
     ap.add_argument("--chunk-cands", type=int, default=None, help="candidates per chunk (default: the engine's)")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU route runs")
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds the CPU baseline mine may run")
+    ap.add_argument("--ref-budget", type=float, default=None,
+                    help="reference arm: seconds each step's mine may run (default: 180 / steps, within 20..90)")
+    ap.add_argument("--no-side", action="store_true", help="skip the plain small and deep sparse side workloads")
     ap.add_argument("--no-pipeline", action="store_true",
                     help="project and count chunks in turn on one stream (per-kernel times without overlap)")
     args = ap.parse_args()
@@ -602,9 +718,17 @@ def main() -> None:
     recorded = LEVEL_CANDIDATES.get(args.workload)
     if recorded is not None:
         assert level_cands == recorded, (level_cands, recorded)
+    side = []
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_estimate(spec, level_cands, bv_host=bv[:128].view(torch.int64).cpu().numpy().view(np.uint64),
-                           workers=max(1, os.cpu_count() or 1))
+        workers = max(1, os.cpu_count() or 1)
+        csr, build_s = dense_k2_host_csr(pkg, spec, workers)
+        run = cpu_route_timed(csr, n_rows, spec["min_support"], spec["max_length"], args.cpu_budget, workers)
+        cpu = _baseline_entry(run, workers, ROUTE_SAMPLE + f", {args.cpu_budget:.0f} s budget")
+        cpu["input_build_s"] = build_s
+        del csr, run
+    if rank == 0 and world == 1 and not args.no_side:
+        side.append(transactions_line(pkg, "plain_small_tx", max(3, args.steps), 3, with_cpu=not args.no_cpu))
+        side.append(deep_sparse_line(pkg, lib, max(2, args.steps), 2, with_cpu=not args.no_cpu))
 
     if rank == 0:
         line = {
@@ -626,6 +750,7 @@ def main() -> None:
             "roofline": roof,
             "kernels": kern,
             "cpu_baseline": cpu,
+            "workloads": side,
             "gpu_launches": launches,
             "clocks": clk,
         }

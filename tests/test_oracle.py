@@ -59,3 +59,38 @@ def test_digest_is_order_free():
     a = [(np.array([[0, 1], [0, 2]], np.int32), np.array([5, 4]))]
     b = [(np.array([[0, 2], [0, 1]], np.int32), np.array([4, 5]))]
     assert miner.digest(a) == miner.digest(b)
+
+
+def test_cpu_route_matches_the_golden_results(pkg, golden_cases):
+    """The restated CPU route (sparse Gram K=2, prefix-group projection Grams K>=3, thread pool) reproduces
+    the golden digest of every case, unbounded (the 1M-row wide-vocabulary case is left to the GPU tests for
+    time: its route mine alone takes about 20 s here)."""
+    from oracle import cpu_route, miner
+    from tests.conftest import case_input
+
+    checked = 0
+    for case in golden_cases.values():
+        if case["name"].startswith("wide_vocab"):
+            continue
+        indptr, items, n_rows = case_input(pkg, case)
+        csr = miner.transaction_csr(indptr, items, n_rows, case["min_support"])
+        if csr is None:
+            continue
+        got = cpu_route.mine(csr.indptr, csr.cols, csr.n_cols, n_rows, case["min_support"], case["max_length"],
+                             prune_equal_support=case["prune_equal_support"],
+                             use_generator_pruning=case["use_generator_pruning"], workers=3)
+        assert got.complete
+        assert miner.digest(got.levels, csr.items) == case["digest"], case["name"]
+        checked += 1
+    assert checked >= 30
+
+
+def test_cpu_route_budget_stops_early_and_says_so(pkg):
+    """With a time budget that has already run out the route counts K=1 only and reports itself incomplete."""
+    from oracle import cpu_route, miner
+
+    t = pkg.synthetic.plain_small(n_rows=20_000, seed=1)
+    csr = miner.transaction_csr(t.indptr, t.items, t.n_rows, 0.01)
+    r = cpu_route.mine(csr.indptr, csr.cols, csr.n_cols, t.n_rows, 0.01, None, workers=2, budget_s=0.0)
+    assert not r.complete
+    assert r.counted[0]["k"] == 1 and r.counted[1]["counted"] == 0

@@ -76,10 +76,14 @@ def test_reference_arm_line_on_cpu():
 
     env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
     r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--workload", "dense_k2_small",
-                        "--steps", "1", "--warmup", "1"], capture_output=True, text=True, env=env, timeout=600)
+                        "--steps", "1", "--warmup", "1", "--ref-budget", "5"], capture_output=True, text=True, env=env,
+                       timeout=600)
     assert r.returncode == 0, r.stderr
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "s"
     assert line["higher_is_better"] is False
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    # A bounded run reports what it measured: a lower bound with the candidates it counted, or the whole mine.
+    assert line["lower_bound"] == line["cpu_baseline"]["lower_bound"]
+    assert line["cpu_baseline"]["counted"][0]["k"] == 1
     assert line["e2e"] == {"value": line["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
