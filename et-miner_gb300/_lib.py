@@ -114,6 +114,15 @@ SIGNATURES: dict[str, tuple] = {
     "etm_device_status": (ctypes.c_int, [_P]),
     "etm_level_compact": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _P, _P, _P, _I64, _I64, _I32, _P, _P, _I64, _P, _P, _I64, _P]),
     "etm_level_compact_static": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _P, _P, _P, _I64, _I64, _I32, _P, _P, _I64, _P, _P]),
+    "etm_count_tiles_sel": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P,
+                                           _P]),
+    "etm_count_cands_sel": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P,
+                                           _P]),
+    "etm_count_tiles_proj_sel": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P, _P]),
+    "etm_classify_sel": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _P, _P, _I64, _I64, _I32, _I32, _P, _P, _P, _P]),
+    "etm_threshold_bits": (ctypes.c_int, [_P, _P, _I64, _I32, _P, _P]),
+    "etm_level_compact_bits": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _P, _P, _P, _I64, _I64, _P, _P, _I64, _P, _P, _I64,
+                                              _P]),
     "etm_level_subsets": (ctypes.c_int, [_P, _P, _I64, _I32, _P, _P, _I64, _P, _P, _P]),
     "etm_select_rows": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I32, _P, _P, _P, _P, _I64, _P, _P, _I64, _P]),
 }

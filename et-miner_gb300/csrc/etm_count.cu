@@ -17,6 +17,17 @@ namespace {
 
 using namespace etm;
 
+// A candidate's count: every count (surv == nullptr), or only a count reaching min_count, with bit t of
+// the survivor bitmask set (the fused threshold of count_shared_tiled_fused, shared_tiled.cu:246-280).
+__device__ __forceinline__ void emit_count(int32_t* out, uint32_t* surv, int64_t t, int32_t v, int32_t min_count) {
+    if (surv == nullptr) {
+        out[t] = v;
+    } else if (v >= min_count) {
+        out[t] = v;
+        atomicOr(surv + (t >> 5), 1u << (t & 31));
+    }
+}
+
 constexpr int TT = 64;                 // suffixes per tile side
 constexpr int WCH = 32;                // words per shared-memory slab
 constexpr int TILE_THREADS = 256;      // 16 x 16 threads, 4 x 4 pairs each
@@ -43,7 +54,7 @@ __global__ void __launch_bounds__(TILE_THREADS) count_tiles_popc_kernel(
     const int64_t* __restrict__ cwords, const int64_t* __restrict__ cld, const int32_t* __restrict__ rows, int width,
     const int64_t* __restrict__ grp_first, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
     const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
-    const uint8_t* __restrict__ cls, int32_t* __restrict__ out) {
+    const uint8_t* __restrict__ cls, int32_t* __restrict__ out, int32_t min_count, uint32_t* __restrict__ surv) {
     __shared__ TileShared sh;
     const int tid = threadIdx.x;
     const int ty = tid >> 4, tx = tid & 15;
@@ -151,7 +162,7 @@ __global__ void __launch_bounds__(TILE_THREADS) count_tiles_popc_kernel(
                 const int64_t j = tj * TT + tx + 16 * c;
                 if (i < j && j < m) {
                     const int64_t t = cb + tri_index(i, j, m);
-                    if (cls == nullptr || cls[t] == ETM_CAND_COUNT) out[t] = (int32_t)acc[r][c];
+                    if (cls == nullptr || cls[t] == ETM_CAND_COUNT) emit_count(out, surv, t, (int32_t)acc[r][c], min_count);
                 }
             }
         }
@@ -169,7 +180,7 @@ __global__ void __launch_bounds__(CAND_THREADS) count_cands_kernel(
     const uint64_t* __restrict__ fbv, int64_t ld, int64_t n_words, const int32_t* __restrict__ rows, int width,
     const int64_t* __restrict__ grp_first, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
     const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
-    const uint8_t* __restrict__ cls, int32_t* __restrict__ out) {
+    const uint8_t* __restrict__ cls, int32_t* __restrict__ out, int32_t min_count, uint32_t* __restrict__ surv) {
     __shared__ int32_t cols_sh[CAND_THREADS / 32][MAXK];
     const int lane = threadIdx.x & 31;
     int32_t* cols = cols_sh[threadIdx.x >> 5];
@@ -202,7 +213,7 @@ __global__ void __launch_bounds__(CAND_THREADS) count_cands_kernel(
             s += __popcll(x.x) + __popcll(x.y);
         }
         s = __reduce_add_sync(0xffffffffu, s);
-        if (lane == 0) out[t] = (int32_t)s;
+        if (lane == 0) emit_count(out, surv, t, (int32_t)s, min_count);
     }
 }
 
@@ -213,12 +224,14 @@ namespace etm {
 int count_tiles_popcount(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
                          const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
                          const int64_t* work_groups, const int64_t* work_off, int64_t n_work, int64_t chunk_base,
-                         const uint8_t* cls, int32_t* out, int64_t n_tiles_hint, cudaStream_t s) {
+                         const uint8_t* cls, int32_t* out, int64_t n_tiles_hint, cudaStream_t s, int32_t min_count,
+                         uint32_t* surv) {
     const int64_t cap = (int64_t)max(1, sm_count()) * 6;
     const int grid = (int)max64(1, min64(cap, n_tiles_hint > 0 ? n_tiles_hint : cap));
     count_tiles_popc_kernel<false><<<grid, TILE_THREADS, 0, s>>>(fbv, ld, n_words, nullptr, nullptr, nullptr, rows,
                                                                  width, grp_first, grp_size, cand_off, work_groups,
-                                                                 work_off, n_work, chunk_base, cls, out);
+                                                                 work_off, n_work, chunk_base, cls, out, min_count,
+                                                                 surv);
     ETM_LAUNCHED("count_tiles_popc");
     return ETM_OK;
 }
@@ -226,11 +239,11 @@ int count_tiles_popcount(const uint64_t* fbv, int64_t ld, int64_t n_words, const
 int count_tiles_proj_popcount(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                               const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
                               const int64_t* work_off, int64_t n_work, int64_t chunk_base, const uint8_t* cls,
-                              int32_t* out, cudaStream_t s) {
+                              int32_t* out, cudaStream_t s, int32_t min_count, uint32_t* surv) {
     const int grid = max(1, sm_count()) * 6;
     count_tiles_popc_kernel<true><<<grid, TILE_THREADS, 0, s>>>(cbuf, 0, 0, cbase, cwords, cld, nullptr, 1, nullptr,
                                                                 grp_size, cand_off, work_groups, work_off, n_work,
-                                                                chunk_base, cls, out);
+                                                                chunk_base, cls, out, min_count, surv);
     ETM_LAUNCHED("count_tiles_proj_popc");
     return ETM_OK;
 }
@@ -252,7 +265,23 @@ extern "C" int etm_count_tiles(const uint64_t* fbv, int64_t ld, int64_t n_words,
                                        work_off, n_work, chunk_base, cls, out_counts, s);
     ETM_REQUIRE(method == ETM_METHOD_POPCOUNT, ETM_EINVAL, "etm_count_tiles: unknown method %d", method);
     return etm::count_tiles_popcount(fbv, ld, n_words, rows, width, grp_first, grp_size, cand_off, work_groups,
-                                     work_off, n_work, chunk_base, cls, out_counts, -1, s);
+                                     work_off, n_work, chunk_base, cls, out_counts, -1, s, 0, nullptr);
+}
+
+extern "C" int etm_count_tiles_sel(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows,
+                                   int32_t width, const int64_t* grp_first, const int32_t* grp_size,
+                                   const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
+                                   int64_t n_work, int64_t chunk_base, const uint8_t* cls, int32_t min_count,
+                                   int32_t* out_counts, uint32_t* surv_bits, void* stream) {
+    ETM_REQUIRE(width >= 1 && width <= MAXP, ETM_EINVAL, "etm_count_tiles_sel: width %d out of range", width);
+    ETM_REQUIRE(ld % WCH == 0 && ld >= n_words, ETM_EINVAL, "etm_count_tiles_sel: ld must be a multiple of %d >= n_words",
+                WCH);
+    ETM_REQUIRE((reinterpret_cast<uintptr_t>(fbv) & 15) == 0, ETM_EINVAL, "etm_count_tiles_sel: fbv must be 16-byte aligned");
+    ETM_REQUIRE(surv_bits != nullptr, ETM_EINVAL, "etm_count_tiles_sel: surv_bits is required");
+    if (n_work <= 0) return ETM_OK;
+    return etm::count_tiles_popcount(fbv, ld, n_words, rows, width, grp_first, grp_size, cand_off, work_groups,
+                                     work_off, n_work, chunk_base, cls, out_counts, -1, as_stream(stream), min_count,
+                                     surv_bits);
 }
 
 extern "C" int etm_count_cands(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
@@ -266,7 +295,25 @@ extern "C" int etm_count_cands(const uint64_t* fbv, int64_t ld, int64_t n_words,
     const int grid = max(1, sm_count()) * 8;
     count_cands_kernel<<<grid, CAND_THREADS, 0, as_stream(stream)>>>(fbv, ld, n_words, rows, width, grp_first, grp_size,
                                                                      cand_off, work_groups, work_off, n_work,
-                                                                     chunk_base, cls, out_counts);
+                                                                     chunk_base, cls, out_counts, 0, nullptr);
+    ETM_LAUNCHED("count_cands");
+    return ETM_OK;
+}
+
+extern "C" int etm_count_cands_sel(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows,
+                                   int32_t width, const int64_t* grp_first, const int32_t* grp_size,
+                                   const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
+                                   int64_t n_work, int64_t chunk_base, const uint8_t* cls, int32_t min_count,
+                                   int32_t* out_counts, uint32_t* surv_bits, void* stream) {
+    ETM_REQUIRE(width >= 1 && width < MAXK, ETM_EINVAL, "etm_count_cands_sel: width %d out of range", width);
+    ETM_REQUIRE(ld % 2 == 0 && ld >= n_words, ETM_EINVAL, "etm_count_cands_sel: ld must be even and >= n_words");
+    ETM_REQUIRE((reinterpret_cast<uintptr_t>(fbv) & 15) == 0, ETM_EINVAL, "etm_count_cands_sel: fbv must be 16-byte aligned");
+    ETM_REQUIRE(surv_bits != nullptr, ETM_EINVAL, "etm_count_cands_sel: surv_bits is required");
+    if (n_work <= 0) return ETM_OK;
+    const int grid = max(1, sm_count()) * 8;
+    count_cands_kernel<<<grid, CAND_THREADS, 0, as_stream(stream)>>>(fbv, ld, n_words, rows, width, grp_first, grp_size,
+                                                                     cand_off, work_groups, work_off, n_work,
+                                                                     chunk_base, cls, out_counts, min_count, surv_bits);
     ETM_LAUNCHED("count_cands");
     return ETM_OK;
 }

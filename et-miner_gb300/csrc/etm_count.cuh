@@ -8,12 +8,13 @@ namespace etm {
 int count_tiles_popcount(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
                          const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
                          const int64_t* work_groups, const int64_t* work_off, int64_t n_work, int64_t chunk_base,
-                         const uint8_t* cls, int32_t* out, int64_t n_tiles_hint, cudaStream_t s);
+                         const uint8_t* cls, int32_t* out, int64_t n_tiles_hint, cudaStream_t s, int32_t min_count,
+                         uint32_t* surv);
 
 int count_tiles_proj_popcount(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                               const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
                               const int64_t* work_off, int64_t n_work, int64_t chunk_base, const uint8_t* cls,
-                              int32_t* out, cudaStream_t s);
+                              int32_t* out, cudaStream_t s, int32_t min_count, uint32_t* surv);
 
 int proj_status_take(cudaStream_t s, int* out);
 // The projection's first wait for a member's bulk copies, in ns (negative: the default; 0: give up at once).

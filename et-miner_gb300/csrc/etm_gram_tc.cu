@@ -380,7 +380,10 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
                 for (int q = 0; q < BW; q++) cur[q] = nxt[q];
             }
             // ---- epilogue: warp w reads lanes 32 (w % 4) .. of accumulator w / 8, columns 128 ((w / 4) % 2) .. ----
-            const bool ok = n_stages == 0 || mbar_wait(&acc_bar, tile_iter & 1u, abort_flag, WAIT_NS);
+            // Warp-uniform, as the tcgen05.ld below needs the whole warp: lane 0 waits for the warp.
+            int acc_ready = 1;
+            if (lane == 0 && n_stages > 0) acc_ready = mbar_wait(&acc_bar, tile_iter & 1u, abort_flag, WAIT_NS);
+            const bool ok = __shfl_sync(0xffffffffu, acc_ready, 0) != 0;
             if (ok) {
                 tc_fence_after();
                 const int lane_base = (warp & 3) * 32;

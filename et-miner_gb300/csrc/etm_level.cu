@@ -131,7 +131,8 @@ __global__ void classify_kernel(const int32_t* __restrict__ rows, int width, int
                                 const int32_t* __restrict__ counts, const uint8_t* __restrict__ free_flags,
                                 const int64_t* __restrict__ grp_first, const int32_t* __restrict__ grp_size,
                                 const int64_t* __restrict__ cand_off, int64_t g0, int64_t g1, int mode,
-                                uint8_t* __restrict__ out_cls, int32_t* __restrict__ out_counts) {
+                                uint8_t* __restrict__ out_cls, int32_t* __restrict__ out_counts, int32_t min_count,
+                                uint32_t* __restrict__ surv) {
     const int64_t base = cand_off[g0];
     const int64_t n = cand_off[g1] - base;
     const bool prune = mode & ETM_SUBSET_PRUNE, infer = (mode & ETM_SUBSET_INFER) && free_flags && counts;
@@ -162,6 +163,7 @@ __global__ void classify_kernel(const int32_t* __restrict__ rows, int width, int
             if (not_free) {
                 cls = ETM_CAND_INFER;
                 out_counts[t] = lowest;
+                if (surv != nullptr && lowest >= min_count) atomicOr(surv + (t >> 5), 1u << (t & 31));
             }
         }
         out_cls[t] = cls;
@@ -202,6 +204,48 @@ struct EmitSurvivor {
         for (int q = 0; q < width; q++) o[q] = ri[q];
         o[width] = rows[(first + c.j) * width + width - 1];
         out_counts[off] = counts[t];
+    }
+};
+
+// Survivor bits of a counted chunk from its dense counts: one thread per 32-candidate word.
+__global__ void threshold_bits_kernel(const int32_t* __restrict__ counts, const uint8_t* __restrict__ cls, int64_t n,
+                                      int32_t min_count, uint32_t* __restrict__ surv) {
+    const int64_t n_w = (n + 31) >> 5;
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n_w; w += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t bits = 0;
+        const int64_t t0 = w << 5;
+        const int nb = (int)min64(32, n - t0);
+        for (int b = 0; b < nb; b++) {
+            const int64_t t = t0 + b;
+            const bool keep = counts[t] >= min_count && (cls == nullptr || cls[t] != ETM_CAND_SKIP);
+            bits |= (keep ? 1u : 0u) << b;
+        }
+        surv[w] = bits;
+    }
+}
+
+// Ordered compaction over a survivor bitmask: the scan runs over 32-candidate words.
+struct WordSurvivors {
+    const uint32_t* surv;
+    int64_t n;
+    __device__ uint32_t bits(int64_t w) const {
+        const int64_t t0 = w << 5;
+        if (t0 >= n) return 0u;
+        const uint32_t b = surv[w];
+        return n - t0 >= 32 ? b : b & ((1u << (n - t0)) - 1u);
+    }
+    __device__ int64_t operator()(int64_t w) const { return __popc(bits(w)); }
+};
+
+struct EmitWordSurvivors {
+    WordSurvivors words;
+    EmitSurvivor emit;
+    __device__ void operator()(int64_t w, int64_t off) const {
+        uint32_t b = words.bits(w);
+        while (b) {
+            emit((w << 5) + (__ffs(b) - 1), off++);
+            b &= b - 1u;
+        }
     }
 };
 
@@ -301,9 +345,47 @@ extern "C" int etm_classify(const int32_t* rows, int32_t width, int64_t n_rows, 
     ETM_REQUIRE(g0 >= 0 && g1 >= g0, ETM_EINVAL, "etm_classify: bad group range");
     if (g1 == g0) return ETM_OK;
     classify_kernel<<<max(1, sm_count()) * 8, 256, 0, as_stream(stream)>>>(
-        rows, width, n_rows, counts, free_flags, grp_first, grp_size, cand_off, g0, g1, mode, out_cls, out_counts);
+        rows, width, n_rows, counts, free_flags, grp_first, grp_size, cand_off, g0, g1, mode, out_cls, out_counts, 0,
+        nullptr);
     ETM_LAUNCHED("classify");
     return ETM_OK;
+}
+
+extern "C" int etm_classify_sel(const int32_t* rows, int32_t width, int64_t n_rows, const int32_t* counts,
+                                const uint8_t* free_flags, const int64_t* grp_first, const int32_t* grp_size,
+                                const int64_t* cand_off, int64_t g0, int64_t g1, int32_t mode, int32_t min_count,
+                                uint8_t* out_cls, int32_t* out_counts, uint32_t* surv_bits, void* stream) {
+    ETM_REQUIRE(width >= 1 && width < MAXK, ETM_EINVAL, "etm_classify_sel: width %d out of range", width);
+    ETM_REQUIRE(g0 >= 0 && g1 >= g0, ETM_EINVAL, "etm_classify_sel: bad group range");
+    ETM_REQUIRE(surv_bits != nullptr, ETM_EINVAL, "etm_classify_sel: surv_bits is required");
+    if (g1 == g0) return ETM_OK;
+    classify_kernel<<<max(1, sm_count()) * 8, 256, 0, as_stream(stream)>>>(
+        rows, width, n_rows, counts, free_flags, grp_first, grp_size, cand_off, g0, g1, mode, out_cls, out_counts,
+        min_count, surv_bits);
+    ETM_LAUNCHED("classify");
+    return ETM_OK;
+}
+
+extern "C" int etm_threshold_bits(const int32_t* counts, const uint8_t* cls, int64_t n_cands, int32_t min_count,
+                                  uint32_t* surv_bits, void* stream) {
+    ETM_REQUIRE(n_cands >= 0, ETM_EINVAL, "etm_threshold_bits: negative n_cands");
+    if (n_cands == 0) return ETM_OK;
+    threshold_bits_kernel<<<grid_for((n_cands + 31) / 32, 256), 256, 0, as_stream(stream)>>>(counts, cls, n_cands,
+                                                                                            min_count, surv_bits);
+    ETM_LAUNCHED("threshold_bits");
+    return ETM_OK;
+}
+
+extern "C" int etm_level_compact_bits(const uint32_t* surv_bits, const int32_t* counts, int64_t n_cands,
+                                      const int32_t* rows, int32_t width, const int64_t* grp_first,
+                                      const int32_t* grp_size, const int64_t* cand_off, int64_t g0, int64_t g1,
+                                      int32_t* out_rows, int32_t* out_counts, int64_t cap, int64_t* acc, int64_t* ws,
+                                      int64_t ws_words, void* stream) {
+    ETM_REQUIRE(width >= 1 && width + 1 < MAXK, ETM_EINVAL, "etm_level_compact_bits: width %d out of range", width);
+    if (n_cands <= 0) return ETM_OK;
+    WordSurvivors words{surv_bits, n_cands};
+    EmitSurvivor emit{counts, rows, width, grp_first, grp_size, cand_off, g0, g1, out_rows, out_counts, cap};
+    return scan_apply((n_cands + 31) / 32, words, EmitWordSurvivors{words, emit}, ws, ws_words, acc, as_stream(stream));
 }
 
 extern "C" int etm_level_compact(const int32_t* counts, const uint8_t* cls, int64_t n_cands, const int32_t* rows,

@@ -537,5 +537,18 @@ extern "C" int etm_count_tiles_proj(const uint64_t* cbuf, const int64_t* cbase, 
     if (n_work <= 0) return ETM_OK;
     ETM_REQUIRE(method == ETM_METHOD_POPCOUNT, ETM_EINVAL, "etm_count_tiles_proj: method %d not available", method);
     return etm::count_tiles_proj_popcount(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work,
-                                          chunk_base, cls, out_counts, as_stream(stream));
+                                          chunk_base, cls, out_counts, as_stream(stream), 0, nullptr);
+}
+
+extern "C" int etm_count_tiles_proj_sel(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords,
+                                        const int64_t* cld, const int32_t* grp_size, const int64_t* cand_off,
+                                        const int64_t* work_groups, const int64_t* work_off, int64_t n_work,
+                                        int64_t chunk_base, const uint8_t* cls, int32_t min_count, int32_t* out_counts,
+                                        uint32_t* surv_bits, void* stream) {
+    ETM_REQUIRE((reinterpret_cast<uintptr_t>(cbuf) & 15) == 0, ETM_EINVAL,
+                "etm_count_tiles_proj_sel: cbuf must be 16-byte aligned");
+    ETM_REQUIRE(surv_bits != nullptr, ETM_EINVAL, "etm_count_tiles_proj_sel: surv_bits is required");
+    if (n_work <= 0) return ETM_OK;
+    return etm::count_tiles_proj_popcount(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work,
+                                          chunk_base, cls, out_counts, as_stream(stream), min_count, surv_bits);
 }

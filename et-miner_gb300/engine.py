@@ -268,7 +268,8 @@ class Engine:
     def __init__(self, device: torch.device | int | None = None, *, method: str = DEFAULT_METHOD,
                  form: str = "batched", chunk_cands: int = CHUNK_CANDS, small_group: int = SMALL_GROUP,
                  project: bool = True, proj_density: float = PROJ_DENSITY, proj_bytes: int = PROJ_BYTES,
-                 tc_elem: int = DEFAULT_TC_ELEM, pipeline: bool = True, autotune: "Autotuner | bool | None" = None):
+                 tc_elem: int = DEFAULT_TC_ELEM, pipeline: bool = True, autotune: "Autotuner | bool | None" = None,
+                 fused: bool = True):
         if not torch.cuda.is_available():
             raise RuntimeError("the GB300 engine needs a CUDA device; there is no CPU fallback")
         self.lib = load_library()
@@ -291,6 +292,9 @@ class Engine:
         self.tc_elem = int(tc_elem)
         #: Batched form: project chunk c+1 on a side stream while chunk c is counted.
         self.pipeline = bool(pipeline)
+        #: Fused threshold: the counting kernels write only the counts reaching min_count and a survivor bit each;
+        #: compaction scans the bitmask (a 32nd of the dense counts). False: dense counts, dense compaction.
+        self.fused = bool(fused)
         #: K=2 counts row-wise from the transactions (when given) while
         #: sum C(len,2) / (pairs x words) is below this (gpu/row_split_chunks.py:130-142); 0 disables.
         self.k2_rows_max_r = K2_ROWS_MAX_R
@@ -436,40 +440,51 @@ class Engine:
                     nbytes=int((m * ((cnt + 63) // 64)).sum() * 8),
                     macs=float((m * (m - 1) / 2 * cnt.astype(np.float64)).sum()))
 
-    def _count_prepped(self, prep, grp_size, cand_off, base, cls, counts, method):
+    def _count_prepped(self, prep, grp_size, cand_off, base, cls, counts, method, sel=None):
         """The tile-pair counts of a prepared projection (one launch on the current stream)."""
         prep["d"].record_stream(torch.cuda.current_stream())
         self._count_words(prep["cbuf"], prep["cbase"], prep["cwords"], prep["cld"], grp_size, cand_off, prep["wg"],
                           prep["wo"], prep["n"], prep["n_tiles"], base, cls, counts, method, prep["nbytes"],
-                          prep["macs"])
+                          prep["macs"], sel)
 
     def _count_projected(self, fbv, ldp, n_words, gen, grp_first, grp_size, cand_off, gids, sizes, pcnt, base, cls,
-                         counts, method):
+                         counts, method, sel=None):
         """Row lists, projected suffix words and tile-pair counts of the listed groups (one launch each)."""
         prep = self._prep_projected(fbv, ldp, n_words, gen, grp_first, grp_size, gids, sizes, pcnt, method)
-        self._count_prepped(prep, grp_size, cand_off, base, cls, counts, method)
+        self._count_prepped(prep, grp_size, cand_off, base, cls, counts, method, sel)
 
     def _count_words(self, cbuf, cbase, cwords, cld, grp_size, cand_off, wg, wo, n, n_tiles, base, cls, counts,
-                     method, nbytes, macs):
+                     method, nbytes, macs, sel=None):
         """Tile-pair counts over member words laid out as cbuf[cbase[wi] + i * cld[wi]]: tensor or popcount.
 
         ``macs`` is the useful work: one multiply-add per candidate pair and row (sum of C(m,2) x rows).
+        ``sel`` = (min_count, survivor bitmask) selects the fused-threshold form.
         """
         if method == 1:
             # The work counter lets the Gram's CTAs claim block pairs dynamically (one per engine: the Gram
             # launches of an engine run in turn on its main stream).
             counter = self.scratch.get("tc_work_counter", 1, torch.int64)
-            st = self._launch("gram_tc", nbytes, lambda: self.lib.etm_count_tiles_tc(
-                _p(cbuf), _p(cbase), _p(cwords), _p(cld), _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, n_tiles,
-                base, _p(cls), self.tc_elem, _p(counts), _p(counter), _stream()), flops=2 * macs)
-            check(st, "etm_count_tiles_tc")
+            if sel is None:
+                fn = lambda: self.lib.etm_count_tiles_tc(  # noqa: E731
+                    _p(cbuf), _p(cbase), _p(cwords), _p(cld), _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, n_tiles,
+                    base, _p(cls), self.tc_elem, _p(counts), _p(counter), _stream())
+            else:
+                fn = lambda: self.lib.etm_count_tiles_tc_sel(  # noqa: E731
+                    _p(cbuf), _p(cbase), _p(cwords), _p(cld), _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, n_tiles,
+                    base, _p(cls), self.tc_elem, sel[0], _p(counts), _p(sel[1]), _p(counter), _stream())
+            check(self._launch("gram_tc", nbytes, fn, flops=2 * macs), "etm_count_tiles_tc")
             self.used_tensor = True
             self._waits_pending = True
         else:
-            st = self._launch("count_tiles_proj", nbytes, lambda: self.lib.etm_count_tiles_proj(
-                _p(cbuf), _p(cbase), _p(cwords), _p(cld), _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, base,
-                _p(cls), 0, _p(counts), _stream()))
-            check(st, "etm_count_tiles_proj")
+            if sel is None:
+                fn = lambda: self.lib.etm_count_tiles_proj(  # noqa: E731
+                    _p(cbuf), _p(cbase), _p(cwords), _p(cld), _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, base,
+                    _p(cls), 0, _p(counts), _stream())
+            else:
+                fn = lambda: self.lib.etm_count_tiles_proj_sel(  # noqa: E731
+                    _p(cbuf), _p(cbase), _p(cwords), _p(cld), _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, base,
+                    _p(cls), sel[0], _p(counts), _p(sel[1]), _stream())
+            check(self._launch("count_tiles_proj", nbytes, fn), "etm_count_tiles_proj")
         self.launches += 1
 
     def count_level(self, gen: Level, fbv: torch.Tensor, ldp: int, n_words: int, mc: int,
@@ -625,16 +640,30 @@ class Engine:
             n_c = int(offs[g1] - base)
             counts = self.scratch.get("chunk_counts", n_c, torch.int32)
             cls = self.scratch.get("chunk_cls", n_c, torch.uint8) if classify else None
+            k2_rows = width == 1 and self._k2_rows is not None
+            row_wise = k2_rows or k3_rows
+            # Fused threshold: the counting kernels set survivor bits (the row-wise kernels count densely and a
+            # threshold pass sets the bits after them).
+            bits = None
+            if self.fused:
+                bits = self.scratch.get("chunk_bits", (n_c + 31) // 32 + 1, torch.int32)
+                bits.zero_()
+            sel = (mc, bits) if (self.fused and not row_wise) else None
             if classify:
-                check(self._launch("classify", n_c * 5, lambda: self.lib.etm_classify(
-                    _p(gen.rows), width, gen.n, _p(gen.counts), _p(gen.free), _p(grp_first), _p(grp_size),
-                    _p(cand_off), g0, g1, mode, _p(cls), _p(counts), _stream())), "etm_classify")
+                if sel is None:
+                    fn = lambda: self.lib.etm_classify(  # noqa: E731
+                        _p(gen.rows), width, gen.n, _p(gen.counts), _p(gen.free), _p(grp_first), _p(grp_size),
+                        _p(cand_off), g0, g1, mode, _p(cls), _p(counts), _stream())
+                else:
+                    fn = lambda: self.lib.etm_classify_sel(  # noqa: E731
+                        _p(gen.rows), width, gen.n, _p(gen.counts), _p(gen.free), _p(grp_first), _p(grp_size),
+                        _p(cand_off), g0, g1, mode, mc, _p(cls), _p(counts), _p(bits), _stream())
+                check(self._launch("classify", n_c * 5, fn), "etm_classify")
                 self.launches += 1
             m = sizes[g0:g1]
             ids = np.arange(g0, g1, dtype=np.int64)
             small = m <= self.small_group
             pr = proj[g0:g1]
-            k2_rows = width == 1 and self._k2_rows is not None
             if k2_rows:
                 stats.row_wise = True
                 # K=2 from the transactions (one group of every generator): pair counts by row-wise increments.
@@ -655,21 +684,21 @@ class Engine:
                                       _p(cand_off), base, n_c, _p(cls), _p(counts), _stream()))
                 check(st, "etm_triple_counts_rows")
                 self.launches += 2
-            for kind, sel in (() if (k2_rows or k3_rows) else
-                              (("cands", small), ("tiles", ~small & ~pr), ("proj", pr & ~small))):
-                gids = ids[sel]
+            for kind, which in (() if (k2_rows or k3_rows) else
+                                (("cands", small), ("tiles", ~small & ~pr), ("proj", pr & ~small))):
+                gids = ids[which]
                 if len(gids) == 0:
                     continue
                 if kind == "proj":
                     if pipelined:
                         main.wait_event(prep_done[c % 2])
-                        self._count_prepped(preps.pop(c), grp_size, cand_off, base, cls, counts, method)
+                        self._count_prepped(preps.pop(c), grp_size, cand_off, base, cls, counts, method, sel)
                         buf_free[c % 2].record(main)
                         continue
                     groups = [gids] if self.form == "batched" else [gids[q:q + 1] for q in range(len(gids))]
                     for bg in groups:
                         self._count_projected(fbv, ldp, n_words, gen, grp_first, grp_size, cand_off, bg, sizes, pcnt,
-                                              base, cls, counts, method)
+                                              base, cls, counts, method, sel)
                     continue
                 if kind == "tiles" and whole_tc:
                     mg = sizes[gids]
@@ -682,12 +711,12 @@ class Engine:
                     self._count_words(fbv, d[2 * n + 1:3 * n + 1], d[3 * n + 1:4 * n + 1], d[4 * n + 1:5 * n + 1],
                                       grp_size, cand_off, d[:n], d[n:2 * n + 1], n, int(toff[-1]), base, cls, counts,
                                       1, int(mg.sum()) * n_words * 8,
-                                      float((mg * (mg - 1) / 2).astype(np.float64).sum() * n_rows))
+                                      float((mg * (mg - 1) / 2).astype(np.float64).sum() * n_rows), sel)
                     continue
                 if kind == "cands":
-                    w = m[sel] * (m[sel] - 1) // 2
+                    w = m[which] * (m[which] - 1) // 2
                 else:
-                    nt = (m[sel] + TILE - 1) // TILE
+                    nt = (m[which] + TILE - 1) // TILE
                     w = nt * (nt + 1) // 2
                 batches = [(gids, w)] if self.form == "batched" else [(gids[q:q + 1], w[q:q + 1]) for q in range(len(gids))]
                 for bg, bw in batches:
@@ -696,27 +725,52 @@ class Engine:
                     if kind == "cands":
                         # Every candidate reads its k columns.
                         nbytes = int((mg * (mg - 1) // 2).sum()) * (width + 1) * n_words * 8
-                        st = self._launch("count_cands", nbytes, lambda: self.lib.etm_count_cands(
-                            _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
-                            _p(wg), _p(wo), len(bg), base, _p(cls), _p(counts), _stream()))
+                        if sel is None:
+                            fn = lambda: self.lib.etm_count_cands(  # noqa: E731
+                                _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
+                                _p(wg), _p(wo), len(bg), base, _p(cls), _p(counts), _stream())
+                        else:
+                            fn = lambda: self.lib.etm_count_cands_sel(  # noqa: E731
+                                _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
+                                _p(wg), _p(wo), len(bg), base, _p(cls), mc, _p(counts), _p(bits), _stream())
+                        st = self._launch("count_cands", nbytes, fn)
                     else:
                         # Each group's prefix and suffix columns, once (the same-data minimum). Groups that reach
                         # this kind under the tensor method hold more than 2^24 rows (past the f32-exact range
                         # of the Gram), so these tiles always count on the CUDA cores.
                         nbytes = int((mg + width - 1).sum()) * n_words * 8
-                        st = self._launch("count_tiles", nbytes, lambda: self.lib.etm_count_tiles(
-                            _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
-                            _p(wg), _p(wo), len(bg), base, _p(cls), 0, _p(counts), _stream()))
+                        if sel is None:
+                            fn = lambda: self.lib.etm_count_tiles(  # noqa: E731
+                                _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
+                                _p(wg), _p(wo), len(bg), base, _p(cls), 0, _p(counts), _stream())
+                        else:
+                            fn = lambda: self.lib.etm_count_tiles_sel(  # noqa: E731
+                                _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
+                                _p(wg), _p(wo), len(bg), base, _p(cls), mc, _p(counts), _p(bits), _stream())
+                        st = self._launch("count_tiles", nbytes, fn)
                     check(st, f"etm_count_{kind}")
                     self.launches += 1
             if pipelined and c + 1 < len(chunks):
                 prep(c + 1)  # overlaps this chunk's counting and the host wait in its compaction
-            ws = self.scratch.get("ws_compact", scan_words(n_c), torch.int64)
+            if self.fused and row_wise:
+                check(self._launch("threshold_bits", n_c * (5 if classify else 4), lambda: self.lib.etm_threshold_bits(
+                    _p(counts), _p(cls), n_c, mc, _p(bits), _stream())), "etm_threshold_bits")
+                self.launches += 1
+            n_scan = (n_c + 31) // 32 if self.fused else n_c
+            ws = self.scratch.get("ws_compact", scan_words(n_scan), torch.int64)
             while True:
-                st = self._launch("level_compact", n_c * (5 if classify else 4), lambda: self.lib.etm_level_compact(
-                    _p(counts), _p(cls), n_c, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off), g0, g1,
-                    mc, _p(out_rows), _p(out_counts), cap, _p(acc), _p(ws), ws.numel(), _stream()))
-                check(st, "etm_level_compact")
+                if self.fused:
+                    # Reads the bitmask, and the counts of the survivors only.
+                    fn = lambda: self.lib.etm_level_compact_bits(  # noqa: E731
+                        _p(bits), _p(counts), n_c, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
+                        g0, g1, _p(out_rows), _p(out_counts), cap, _p(acc), _p(ws), ws.numel(), _stream())
+                    nbytes = (n_c + 7) // 8
+                else:
+                    fn = lambda: self.lib.etm_level_compact(  # noqa: E731
+                        _p(counts), _p(cls), n_c, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off), g0,
+                        g1, mc, _p(out_rows), _p(out_counts), cap, _p(acc), _p(ws), ws.numel(), _stream())
+                    nbytes = n_c * (5 if classify else 4)
+                check(self._launch("level_compact", nbytes, fn), "etm_level_compact")
                 self.launches += 3
                 new_total = int(acc.item())
                 if new_total <= cap:
@@ -846,5 +900,5 @@ class Engine:
 def mine(bitvecs, n_rows: int, min_support: float, max_length: int | None = None, **kw) -> MineOutput:
     """Mine device bitvectors [n_cols, ceil(N/64)] with a fresh ``Engine`` (see ``Engine.mine``)."""
     engine_kw = {k: kw.pop(k) for k in ("method", "form", "chunk_cands", "small_group", "device", "project",
-                                        "proj_density", "proj_bytes", "tc_elem", "pipeline", "autotune") if k in kw}
+                                        "proj_density", "proj_bytes", "tc_elem", "pipeline", "autotune", "fused") if k in kw}
     return Engine(**engine_kw).mine(bitvecs, n_rows, min_support, max_length, **kw)

@@ -318,6 +318,60 @@ int etm_device_status(void* stream);
 int etm_set_wait_limits(int64_t gram_first_wait_ns, int64_t proj_first_wait_ns);
 
 /*
+ * The fused-threshold ("select") forms of the counting entry points, after
+ * count_shared_tiled_fused (gpu/kernels/_src/shared_tiled.cu:246-280): each
+ * takes min_count and a survivor bitmask surv_bits (uint32 words; bit t % 32
+ * of word t / 32 is chunk-relative candidate t; the caller zeroes
+ * ceil(n_cands / 32) words before the chunk's first call). Of the candidates
+ * a call counts, only those reaching min_count get out_counts[t] written and
+ * their bit set; the other slots are left untouched. etm_classify_sel sets
+ * the bit of an inferred candidate reaching min_count. Arguments otherwise as
+ * in the dense forms (etm_count_tiles with the popcount method,
+ * etm_count_cands, etm_count_tiles_proj, etm_classify).
+ */
+int etm_count_tiles_sel(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                        const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
+                        const int64_t* work_groups, const int64_t* work_off, int64_t n_work, int64_t chunk_base,
+                        const uint8_t* cls, int32_t min_count, int32_t* out_counts, uint32_t* surv_bits,
+                        void* stream);
+int etm_count_cands_sel(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                        const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
+                        const int64_t* work_groups, const int64_t* work_off, int64_t n_work, int64_t chunk_base,
+                        const uint8_t* cls, int32_t min_count, int32_t* out_counts, uint32_t* surv_bits,
+                        void* stream);
+int etm_count_tiles_proj_sel(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
+                             const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
+                             const int64_t* work_off, int64_t n_work, int64_t chunk_base, const uint8_t* cls,
+                             int32_t min_count, int32_t* out_counts, uint32_t* surv_bits, void* stream);
+int etm_classify_sel(const int32_t* rows, int32_t width, int64_t n_rows, const int32_t* counts,
+                     const uint8_t* free_flags, const int64_t* grp_first, const int32_t* grp_size,
+                     const int64_t* cand_off, int64_t g0, int64_t g1, int32_t mode, int32_t min_count,
+                     uint8_t* out_cls, int32_t* out_counts, uint32_t* surv_bits, void* stream);
+
+/*
+ * Survivor bits of a chunk whose counts are dense (the row-wise kernels):
+ * bit t set when counts[t] >= min_count and (cls NULL or cls[t] != SKIP).
+ * Writes every one of the ceil(n_cands / 32) words. Replaces the comparison
+ * half of threshold_filter (gpu/kernels/filter.py:85-120).
+ */
+int etm_threshold_bits(const int32_t* counts, const uint8_t* cls, int64_t n_cands, int32_t min_count,
+                       uint32_t* surv_bits, void* stream);
+
+/*
+ * etm_level_compact over a survivor bitmask instead of dense counts: the
+ * ordered scan runs over the ceil(n_cands / 32) words (a 32nd of the
+ * elements), and each set bit t is decoded into a row of width+1 columns with
+ * count counts[t], in candidate order. acc, cap and the output rules as in
+ * etm_level_compact; ws: ceil(n_cands / 32) / 4096 + 3 words. Replaces
+ * threshold_filter's compaction (gpu/kernels/filter.py:165-237) and the
+ * decode steps (gpu/kernels/decode.py:9-73).
+ */
+int etm_level_compact_bits(const uint32_t* surv_bits, const int32_t* counts, int64_t n_cands, const int32_t* rows,
+                           int32_t width, const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
+                           int64_t g0, int64_t g1, int32_t* out_rows, int32_t* out_counts, int64_t cap,
+                           int64_t* acc, int64_t* ws, int64_t ws_words, void* stream);
+
+/*
  * Survivors of a counted chunk (groups [g0, g1)), in candidate order, decoded
  * into rows of width+1 columns. Replaces threshold_filter
  * (gpu/kernels/filter.py:85-120), decode_k2_pairs_flat / decode_k3plus_flat

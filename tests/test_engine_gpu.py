@@ -43,6 +43,9 @@ def engines(pkg):
         "rows": _rows_engine(eng.Engine()),
         "rows3": _rows_engine(eng.Engine(), k3=True),
         "tuned": eng.Engine(autotune=import_module(pkg.__name__ + ".autotune").Autotuner(min_candidates=1)),
+        "dense": eng.Engine(fused=False),
+        "dense_tiny": eng.Engine(fused=False, chunk_cands=97, small_group=3),
+        "rows_dense": _rows_engine(eng.Engine(fused=False), k3=True),
     }
 
 
@@ -61,7 +64,8 @@ def test_transactions_match_golden(pkg, golden_cases, engines, name):
         assert pairs == want
 
 
-@pytest.mark.parametrize("form", ["plain", "tiny", "proj", "noproj", "popcount", "tuned", "rows", "rows3"])
+@pytest.mark.parametrize("form", ["plain", "tiny", "proj", "noproj", "popcount", "tuned", "rows", "rows3", "dense",
+                                  "dense_tiny", "rows_dense"])
 @pytest.mark.parametrize("name", ["implication_plain", "implication_prune", "implication_infer", "plain_small_plain",
                                   "deep_sparse_small", "dense_k2_small", "word_tail_65"])
 def test_forms_match_golden(pkg, golden_cases, engines, name, form):

@@ -242,6 +242,53 @@ def test_compaction_overflow_regrows(pkg):
     assert np.array_equal(new.counts.cpu().numpy(), want)
 
 
+@pytest.mark.parametrize("n_groups", [1, 5])
+def test_bitmask_compaction_matches_dense_compaction(pkg, lib, n_groups):
+    """etm_threshold_bits + etm_level_compact_bits give the rows, counts and order of etm_level_compact on the
+    same dense counts and classes, for chunk sizes that end inside a 32-candidate word."""
+    import torch
+
+    from importlib import import_module
+
+    engm = import_module(pkg.__name__ + ".engine")
+    eng = engm.Engine()
+    rng = np.random.default_rng(n_groups)
+    # A width-2 level of n_groups prefix groups of uneven sizes: rows (p, s) lexsorted.
+    sizes = rng.integers(2, 90, size=n_groups)
+    rows = np.array([(p, s) for p, m in enumerate(sizes) for s in range(p + 1, p + 1 + m)], np.int32)
+    gen = engm.Level(torch.from_numpy(rows).cuda(), torch.ones(len(rows), dtype=torch.int32, device="cuda"))
+    G, total, grp_first, grp_size, cand_off = eng.groups(gen)
+    assert G == n_groups and total == int((sizes * (sizes - 1) // 2).sum())
+    counts = torch.from_numpy(rng.integers(0, 50, size=total).astype(np.int32)).cuda()
+    cls = torch.from_numpy(rng.choice(np.array([0, 0, 1, 2], np.uint8), size=total)).cuda()
+    s0 = torch.cuda.current_stream().cuda_stream
+    outs = []
+    for fused in (False, True):
+        out_r = torch.full((total, 3), -1, dtype=torch.int32, device="cuda")
+        out_c = torch.full((total,), -1, dtype=torch.int32, device="cuda")
+        acc = torch.zeros(1, dtype=torch.int64, device="cuda")
+        if fused:
+            bits = torch.full(((total + 31) // 32 + 1,), -1, dtype=torch.int32, device="cuda")
+            assert lib.etm_threshold_bits(counts.data_ptr(), cls.data_ptr(), total, 25, bits.data_ptr(), s0) == 0
+            ws = torch.empty(engm.scan_words((total + 31) // 32), dtype=torch.int64, device="cuda")
+            st = lib.etm_level_compact_bits(bits.data_ptr(), counts.data_ptr(), total, gen.rows.data_ptr(), 2,
+                                            grp_first.data_ptr(), grp_size.data_ptr(), cand_off.data_ptr(), 0, G,
+                                            out_r.data_ptr(), out_c.data_ptr(), total, acc.data_ptr(), ws.data_ptr(),
+                                            ws.numel(), s0)
+        else:
+            ws = torch.empty(engm.scan_words(total), dtype=torch.int64, device="cuda")
+            st = lib.etm_level_compact(counts.data_ptr(), cls.data_ptr(), total, gen.rows.data_ptr(), 2,
+                                       grp_first.data_ptr(), grp_size.data_ptr(), cand_off.data_ptr(), 0, G, 25,
+                                       out_r.data_ptr(), out_c.data_ptr(), total, acc.data_ptr(), ws.data_ptr(),
+                                       ws.numel(), s0)
+        assert st == 0, lib.etm_last_error()
+        n = int(acc.item())
+        outs.append((out_r[:n].cpu().numpy(), out_c[:n].cpu().numpy()))
+    keep = (counts.cpu().numpy() >= 25) & (cls.cpu().numpy() != 1)
+    assert len(outs[0][1]) == int(keep.sum()) > 0
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
 @pytest.mark.parametrize("max_len", [20, 700])
 def test_pair_counts_rows_match_host(pkg, lib, max_len):
     """Row-wise K=2 (pairs_k2_rows.cu:54 restated): every pair count from the rows, through a column lut."""
