@@ -479,6 +479,18 @@ def run_serving(args) -> None:
         results = [f.result() for f in futs]
         makespan = time.perf_counter() - t1
         st = server.stats()
+    # Capacity: the same requests all queued at once (arrival times ignored), merged and one mine each.
+    capacity = {}
+    for name, ratio in (("merged", 2.0), ("one_mine_per_request", 1.0)):
+        with serve.Server(datasets, slots=args.slots, merge_ratio=ratio) as server:
+            t2 = time.perf_counter()
+            futs_c = [server.submit(r.dataset, r.min_support, r.max_length) for r in reqs]
+            for f in futs_c:
+                f.result()
+            span = time.perf_counter() - t2
+            sc = server.stats()
+        capacity[name] = {"requests_per_s": len(reqs) / span, "makespan_s": span, "mines": sc["mines"],
+                          "p50_s": sc["p50_s"], "p99_s": sc["p99_s"]}
     clk = clocks.stop()
     # Exactness: every request against the same request mined alone (one engine, nothing else on the GPU),
     # and the CPU oracle on the small datasets.
@@ -507,6 +519,7 @@ def run_serving(args) -> None:
                    "datasets": [{"rows": ds.n_rows, "items": ds.n_cols} for ds in datasets]},
         "p50_s": st["p50_s"], "p99_s": st["p99_s"], "mean_s": st["mean_s"], "max_s": st["max_s"],
         "queued_p99_s": st["queued_p99_s"], "throughput_rps": len(reqs) / makespan, "makespan_s": makespan,
+        "mines": st["mines"], "capacity": capacity,
         "dataset_build_s": build_s,
         "exact": {"alone_equal": f"{alone_ok}/{len(sample)}", "oracle_equal": f"{oracle_ok}/{oracle_n}"},
         "clocks": clk,

@@ -131,20 +131,39 @@ def _unsupported(**opts) -> None:
 
 # ---- input: transactions -> CSR of frequent columns ------------------------------
 
-def _list_column(transactions, item_col: str) -> tuple[np.ndarray, np.ndarray, np.dtype]:
-    """(indptr int64, flat item values, their numpy dtype) of a transaction list column.
+def _coded(flat: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """(int64 rank of every item among the distinct items, those items sorted): the coding of non-integer
+    item ids (``_coded_items``, core/apriori.py:277-284). Ranks follow the item order, so ascending codes
+    are ascending items; results map back through the sorted items."""
+    labels, codes = np.unique(flat, return_inverse=True)
+    return codes.astype(np.int64).ravel(), labels
+
+
+def _label_values(flat: np.ndarray) -> np.ndarray:
+    """Non-integer items as a result emits them (``_emitted_items``, core/result.py:82-92): floats as
+    float64, anything else (strings, categorical values) as strings."""
+    if np.issubdtype(flat.dtype, np.floating):
+        return flat.astype(np.float64)
+    return flat.astype(str)
+
+
+def _list_column(transactions, item_col: str):
+    """(indptr int64, flat item values, their numpy dtype, labels) of a transaction list column.
 
     Accepts a polars DataFrame/LazyFrame or pyarrow Table (when installed), a
     CSR object with ``indptr`` and ``items`` arrays, a dict ``{item_col: rows}``
     or a list of item lists. Null lists are rows without items; null entries
-    are no items.
+    are no items. Integer ids come back as they are with ``labels`` None;
+    strings, floats and categorical values come back coded (int64 ranks) with
+    ``labels`` the sorted distinct values the ranks stand for.
     """
     if hasattr(transactions, "indptr") and hasattr(transactions, "items") and not isinstance(transactions, dict):
         indptr = np.asarray(transactions.indptr, dtype=np.int64)
         flat = np.asarray(transactions.items)
-        if not np.issubdtype(flat.dtype, np.integer):
-            raise TypeError(f"items must be integer ids on the GPU route, got {flat.dtype}")
-        return indptr, flat, flat.dtype
+        if np.issubdtype(flat.dtype, np.integer):
+            return indptr, flat, flat.dtype, None
+        codes, labels = _coded(_label_values(flat))
+        return indptr, codes, codes.dtype, labels
     if isinstance(transactions, dict):
         return _python_rows(transactions[item_col])
     if isinstance(transactions, (list, tuple)):
@@ -162,8 +181,10 @@ def _list_column(transactions, item_col: str) -> tuple[np.ndarray, np.ndarray, n
         arr = arr.combine_chunks()
     if not (pa.types.is_list(arr.type) or pa.types.is_large_list(arr.type)):
         raise TypeError(f"column {item_col!r} must be a list column, got {arr.type}")
-    if not pa.types.is_integer(arr.type.value_type):
-        raise TypeError(f"items must be integer ids on the GPU route, got {arr.type.value_type}")
+    vt = arr.type.value_type
+    if not (pa.types.is_integer(vt) or pa.types.is_floating(vt) or pa.types.is_string(vt)
+            or pa.types.is_large_string(vt) or pa.types.is_dictionary(vt)):
+        raise TypeError(f"items must be integers, floats, strings or categorical values, got {vt}")
     offsets = np.asarray(arr.offsets.to_numpy(zero_copy_only=False), dtype=np.int64)
     n = len(arr)
     vals = arr.values.slice(offsets[0], offsets[-1] - offsets[0])
@@ -172,23 +193,40 @@ def _list_column(transactions, item_col: str) -> tuple[np.ndarray, np.ndarray, n
         valid &= ~np.asarray(vals.is_null().to_numpy(zero_copy_only=False))
     if arr.null_count:
         valid &= np.repeat(~np.asarray(arr.is_null().to_numpy(zero_copy_only=False)), np.diff(offsets))
-    flat = np.asarray(vals.fill_null(0).to_numpy(zero_copy_only=False))
+    if pa.types.is_dictionary(vt):
+        vals = vals.cast(vt.value_type)  # categorical values are emitted as their strings
+    if pa.types.is_integer(vt):
+        flat = np.asarray(vals.fill_null(0).to_numpy(zero_copy_only=False))
+    else:
+        flat = np.asarray(vals.to_numpy(zero_copy_only=False))
     rid = np.repeat(np.arange(n, dtype=np.int64), np.diff(offsets))[valid]
     indptr = np.zeros(n + 1, dtype=np.int64)
     np.cumsum(np.bincount(rid, minlength=n), out=indptr[1:])
-    return indptr, flat[valid], flat.dtype
+    flat = flat[valid]
+    if pa.types.is_integer(vt):
+        return indptr, flat, flat.dtype, None
+    codes, labels = _coded(_label_values(flat))
+    return indptr, codes, codes.dtype, labels
 
 
-def _python_rows(rows) -> tuple[np.ndarray, np.ndarray, np.dtype]:
+def _python_rows(rows):
     rows = [[] if r is None else [x for x in r if x is not None] for r in rows]
     indptr = np.zeros(len(rows) + 1, dtype=np.int64)
     np.cumsum([len(r) for r in rows], out=indptr[1:])
     flat_list = [x for r in rows for x in r]
-    if any(not isinstance(x, numbers.Integral) for x in flat_list):
-        raise TypeError("items must be integer ids on the GPU route")
-    big = any(x > np.iinfo(np.int64).max for x in flat_list)
-    flat = np.array(flat_list, dtype=np.uint64 if big else np.int64)
-    return indptr, flat, flat.dtype
+    if all(isinstance(x, numbers.Integral) and not isinstance(x, bool) for x in flat_list):
+        big = any(x > np.iinfo(np.int64).max for x in flat_list)
+        flat = np.array(flat_list, dtype=np.uint64 if big else np.int64)
+        return indptr, flat, flat.dtype, None
+    kinds = {type(x) for x in flat_list}
+    if all(issubclass(t, numbers.Real) and not issubclass(t, bool) for t in kinds):
+        flat = np.array(flat_list, dtype=np.float64)
+    elif all(issubclass(t, str) for t in kinds):
+        flat = np.array(flat_list, dtype=str)
+    else:
+        raise TypeError(f"items must all be integers, all numbers or all strings, got {sorted(t.__name__ for t in kinds)}")
+    codes, labels = _coded(_label_values(flat))
+    return indptr, codes, codes.dtype, labels
 
 
 def _frequent_csr(indptr: np.ndarray, flat: np.ndarray, n_rows: int, mc: int):
@@ -318,7 +356,9 @@ class ItemsetFrame:
     def to_arrow(self):
         if pa is None:
             raise ImportError("pyarrow is not installed")
-        item_type = pa.uint64() if self.values.dtype == np.uint64 else pa.int64()
+        kind = self.values.dtype
+        item_type = (pa.uint64() if kind == np.uint64 else pa.float64() if np.issubdtype(kind, np.floating)
+                     else pa.large_string() if kind.kind in "UO" else pa.int64())
         itemset = pa.LargeListArray.from_arrays(pa.array(self.offsets, pa.int64()), pa.array(self.values, item_type))
         return pa.table({"itemset": itemset, "support": pa.array(self.support, pa.float64())})
 
@@ -367,7 +407,11 @@ def result_pairs(result, n_rows: int) -> list[tuple[tuple[int, ...], int]]:
         sets = [tuple(s) for s in table.column("itemset").to_pylist()]
         sup = np.asarray(table.column("support").to_numpy(), dtype=np.float64)
     counts = np.rint(np.asarray(sup, dtype=np.float64) * n_rows).astype(np.int64)
-    out = [(tuple(int(x) for x in s), int(c)) for s, c in zip(sets, counts)]
+
+    def item(x):
+        return int(x) if isinstance(x, (numbers.Integral, np.integer)) else (float(x) if isinstance(x, float) else x)
+
+    out = [(tuple(item(x) for x in s), int(c)) for s, c in zip(sets, counts)]
     out.sort(key=lambda t: (len(t[0]), t[0]))
     return out
 
@@ -394,9 +438,12 @@ def _array_facts(bv) -> tuple[tuple[int, ...], str, bool]:
     return shape, cai["typestr"], contiguous
 
 
-def _emit(out: MineOutput, col_items: np.ndarray):
-    """The result frame; item ids, offsets and supports are built on the device (``frame_arrays``)."""
+def _emit(out: MineOutput, col_items: np.ndarray, labels: np.ndarray | None = None):
+    """The result frame; item ids, offsets and supports are built on the device (``frame_arrays``). With
+    ``labels``, the ids are codes of non-integer items and map back through them."""
     offsets, values, support, _ = out.frame_arrays(col_items)
+    if labels is not None:
+        values = labels[values]
     frame = ItemsetFrame(offsets, values, support)
     if _pl is not None:
         return frame.to_polars()
@@ -496,7 +543,8 @@ def apriori(
         col_items = np.array(vals, dtype=np.uint64 if wide else np.int64)
         out = eng.mine(bv, n_trans, min_support, max_length, prune_equal_support=prune_equal_support,
                        use_generator_pruning=use_generator_pruning, level_callback=level_callback,
-                       n_cols_logical=(max(col_to_item.keys()) + 1) if col_to_item else 0)
+                       n_cols_logical=(max(col_to_item.keys()) + 1) if col_to_item else 0,
+                       max_ram_gb=max_ram_gb, max_vram_gb=max_vram_gb)
         if warn_complexity and out.stats:
             _warn_complexity(out.stats[0].n_frequent, min_support)
         df = _emit(out, col_items)
@@ -506,7 +554,7 @@ def apriori(
 
     if transactions is None:
         raise ValueError("Either 'transactions' or 'bitvecs' must be provided")
-    indptr, flat, kind = _list_column(transactions, item_col)
+    indptr, flat, kind, labels = _list_column(transactions, item_col)
     n_rows = len(indptr) - 1
     if n_rows > np.iinfo(np.int32).max:
         raise ValueError(f"n_transactions={n_rows:,} exceeds int32 max")
@@ -521,10 +569,11 @@ def apriori(
     max_tx = int(np.diff(indptr).max()) if n_rows else 0
     eff = min(max_length, max_tx) if max_length else max_tx
     out = eng.mine(bv, n_rows, min_support, eff if eff >= 1 else 1, prune_equal_support=prune_equal_support,
-                   use_generator_pruning=use_generator_pruning, level_callback=level_callback, rows=rows)
+                   use_generator_pruning=use_generator_pruning, level_callback=level_callback, rows=rows,
+                   max_ram_gb=max_ram_gb, max_vram_gb=max_vram_gb)
     if warn_complexity and out.stats:
         _warn_complexity(out.stats[0].n_frequent, min_support)
-    df = _emit(out, items.astype(np.uint64 if wide else np.int64))
+    df = _emit(out, items.astype(np.uint64 if wide else np.int64), labels)
     if session is not None:
         _session_from(out, session)
     return (df, session) if profile else df

@@ -230,6 +230,33 @@ class _Scratch:
         return t[:n]
 
 
+def host_rss_gb() -> float:
+    """Resident set size of this process in GB (/proc/self/status; 0 where it cannot be read)."""
+    try:
+        with open("/proc/self/status") as f:
+            for line in f:
+                if line.startswith("VmRSS:"):
+                    return int(line.split()[1]) / (1 << 20)
+    except OSError:
+        pass
+    return 0.0
+
+
+def check_memory_guard(k: int, ram_gb: float, vram_gb: float, max_ram_gb: float | None,
+                       max_vram_gb: float | None) -> None:
+    """Raise MemoryError when a level left the process over a memory limit (gpu/row_split.py:467-487): the
+    lattice is incomplete at that point, so it is not returned."""
+    for used, limit, what, remedy in (
+        (ram_gb, max_ram_gb, "RAM", "lower max_length or mine fewer levels per call"),
+        (vram_gb, max_vram_gb, "VRAM", "lower max_length, or lower the engine's chunk and projection budgets"),
+    ):
+        if limit is not None and used > limit:
+            raise MemoryError(
+                f"Memory guard tripped after K={k}: {what}={used:.1f}GB exceeds max_{what.lower()}_gb={limit}GB. "
+                f"The lattice is INCOMPLETE at this point, so it is not returned. Raise max_{what.lower()}_gb, "
+                f"or {remedy}.")
+
+
 def scan_words(n: int) -> int:
     return (max(n, 1) + 4095) // 4096 + 2
 
@@ -834,10 +861,16 @@ class Engine:
     # -- the whole mine ----------------------------------------------------------
     def mine(self, bitvecs, n_rows: int, min_support: float, max_length: int | None = None, *,
              prune_equal_support: bool = False, use_generator_pruning: bool = False,
-             level_callback=None, n_cols_logical: int | None = None, rows=None) -> MineOutput:
+             level_callback=None, n_cols_logical: int | None = None, rows=None, max_ram_gb: float | None = None,
+             max_vram_gb: float | None = None) -> MineOutput:
         """Mine device bitvectors. ``rows`` = (row_ptr int64, cols int32, host row lengths) on the device,
         the transactions the bitvectors were built from, lets K=2 count row-wise when its rows are short
-        against the pair space (the reference's rule, gpu/row_split_chunks.py:124-142)."""
+        against the pair space (the reference's rule, gpu/row_split_chunks.py:124-142).
+
+        ``max_ram_gb`` / ``max_vram_gb``: after every level, the process's resident memory and the device
+        memory allocated through torch (every engine buffer) are checked against them; over a limit the mine raises
+        MemoryError instead of returning a partial lattice (gpu/row_split.py:467-487).
+        """
         ptr, (n_cols, ld), _owner = as_device_bitvecs(bitvecs)
         self._k2_rows = None
         self._rows_input = None
@@ -889,6 +922,9 @@ class Engine:
             out.stats.append(stats)
             if level_callback:
                 level_callback(k, stats.n_candidates, new.n, stats.ms)
+            if max_ram_gb is not None or max_vram_gb is not None:
+                check_memory_guard(k, host_rss_gb(), torch.cuda.memory_allocated(self.device) / (1 << 30),
+                                   max_ram_gb, max_vram_gb)
             if new.n == 0:
                 break
             out.levels.append(new)

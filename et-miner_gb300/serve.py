@@ -9,8 +9,23 @@ on the GPU at once: every slot mines on its own CUDA stream with its own
 on the SMs. A finished request frees its slot and memory, and the queue head
 is admitted immediately (continuous batching, not a queue drained one by one).
 
+Requests on the same dataset share launches: when a slot takes the queue
+head, it also takes the queued requests on that dataset whose thresholds are
+within ``merge_ratio`` of the head's (and that fit the memory budget), mines
+once at the lowest min_count and the longest max_length, and hands each
+request the itemsets that reach its own min_count and length. That is exact:
+the frequent itemsets at a threshold are those of a lower threshold whose
+count reaches it (the free-set prune and generator pruning are not served
+here, so no other rule applies).
+
+Memory: admission uses an estimate of each request's device footprint; each
+mine also runs under the engine's memory guard at the server's budget, so a
+request whose real allocations outgrow the budget fails with MemoryError
+instead of starving the others.
+
 Latency of a request = completion time - arrival time (queueing included);
-``Server.stats()`` reports p50/p99 and throughput.
+``Server.stats()`` reports p50/p99, the span from the first arrival to the
+last completion and the throughput over it.
 
 There is no counterpart in the reference (ET-Miner mines one call at a time).
 """
@@ -70,6 +85,9 @@ class Result:
     latency_s: float
     queued_s: float
     run_s: float
+    arrival: float = 0.0
+    finished: float = 0.0
+    batch: int = 1  # requests served by the same mine
 
 
 def dataset_from_transactions(indptr: np.ndarray, items: np.ndarray, device=None) -> Dataset:
@@ -98,9 +116,13 @@ class Server:
     """
 
     def __init__(self, datasets: list[Dataset], *, slots: int = 4, hbm_budget: int | None = None,
-                 engine_kw: dict | None = None):
+                 engine_kw: dict | None = None, merge_ratio: float = 2.0, max_batch: int = 16):
         self.datasets = datasets
         self.slots = max(1, int(slots))
+        #: Queued requests on the head's dataset join its mine when min_count(head) / min_count(them) is at most
+        #: this (1 disables merging); at most max_batch requests per mine.
+        self.merge_ratio = float(merge_ratio)
+        self.max_batch = max(1, int(max_batch))
         if hbm_budget is None:
             free, _ = torch.cuda.mem_get_info()
             hbm_budget = int(free * 0.8)
@@ -149,21 +171,42 @@ class Server:
             self._lock.notify_all()
         return job.future
 
-    def _take(self) -> Job | None:
+    def _min_count(self, job: Job) -> int:
+        return mining_min_count(job.min_support, self.datasets[job.dataset].n_rows)
+
+    def _take(self) -> list[Job] | None:
+        """The queue head and the queued requests that can share its mine (same dataset, thresholds within
+        merge_ratio), once the batch's footprint fits the unreserved budget."""
         with self._lock:
             while True:
                 if self._stop and not self._queue:
                     return None
-                if self._queue and self._queue[0].footprint + self._reserved <= self.hbm_budget:
-                    job = self._queue.popleft()
-                    self._reserved += job.footprint
-                    self._running += 1
-                    return job
+                if self._queue:
+                    head = self._queue[0]
+                    mc0 = self._min_count(head)
+                    batch = [head]
+                    for job in list(self._queue)[1:]:
+                        if len(batch) >= self.max_batch or self.merge_ratio <= 1.0:
+                            break
+                        if job.dataset == head.dataset and max(mc0, self._min_count(job)) <= self.merge_ratio * min(
+                                mc0, self._min_count(job)):
+                            batch.append(job)
+                    # The mine runs at the batch's lowest threshold: its footprint is that request's.
+                    need = max(j.footprint for j in batch)
+                    if need + self._reserved <= self.hbm_budget:
+                        for j in batch:
+                            self._queue.remove(j)
+                        batch[0].footprint, rest = need, batch[1:]
+                        for j in rest:
+                            j.footprint = 0
+                        self._reserved += need
+                        self._running += 1
+                        return batch
                 self._lock.wait(0.05)
 
-    def _release(self, job: Job) -> None:
+    def _release(self, batch: list[Job]) -> None:
         with self._lock:
-            self._reserved -= job.footprint
+            self._reserved -= sum(j.footprint for j in batch)
             self._running -= 1
             self._lock.notify_all()
 
@@ -172,28 +215,40 @@ class Server:
         stream = torch.cuda.Stream()
         engine = None
         while True:
-            job = self._take()
-            if job is None:
+            batch = self._take()
+            if batch is None:
                 return
             try:
                 with torch.cuda.stream(stream):
                     if engine is None:
                         engine = Engine(**self.engine_kw)
-                    job.started = time.perf_counter()
-                    ds = self.datasets[job.dataset]
-                    out = engine.mine(ds.bitvecs, ds.n_rows, job.min_support, job.max_length)
+                    started = time.perf_counter()
+                    ds = self.datasets[batch[0].dataset]
+                    low = min(batch, key=self._min_count)
+                    lengths = [j.max_length for j in batch]
+                    max_len = None if any(m is None for m in lengths) else max(lengths)
+                    out = engine.mine(ds.bitvecs, ds.n_rows, low.min_support, max_len,
+                                      max_vram_gb=self.hbm_budget / (1 << 30))
                     levels = [(ds.items[cols], counts) for cols, counts in out.host_levels()]
                     stream.synchronize()
-                job.finished = time.perf_counter()
-                res = Result(job.rid, job.dataset, levels, ds.n_rows, job.finished - job.arrival,
-                             job.started - job.arrival, job.finished - job.started)
-                with self._lock:
-                    self._results.append(res)
-                job.future.set_result(res)
-            except BaseException as exc:  # the request fails; the server keeps serving
-                job.future.set_exception(exc)
+                finished = time.perf_counter()
+                for job in batch:
+                    mc = self._min_count(job)
+                    mine = [(sets[keep], counts[keep]) for sets, counts in levels
+                            if job.max_length is None or sets.shape[1] <= job.max_length
+                            for keep in [counts >= mc] if keep.any()]
+                    job.started, job.finished = started, finished
+                    res = Result(job.rid, job.dataset, mine, ds.n_rows, finished - job.arrival,
+                                 started - job.arrival, finished - started, job.arrival, finished, len(batch))
+                    with self._lock:
+                        self._results.append(res)
+                    job.future.set_result(res)
+            except BaseException as exc:  # the requests fail; the server keeps serving
+                for job in batch:
+                    if not job.future.done():
+                        job.future.set_exception(exc)
             finally:
-                self._release(job)
+                self._release(batch)
 
     # -- lifecycle -------------------------------------------------------------
     def close(self, wait: bool = True) -> None:
@@ -217,11 +272,11 @@ class Server:
         if not res:
             return {"requests": 0}
         lat = np.array([r.latency_s for r in res])
-        span = max(r.latency_s + 0 for r in res)
-        first = min(r.latency_s - r.run_s - r.queued_s for r in res)
-        del first
+        span = max(r.finished for r in res) - min(r.arrival for r in res)
         return {
             "requests": len(res),
+            "throughput_rps": len(res) / span if span > 0 else math.nan,
+            "mines": int(sum(1.0 / r.batch for r in res) + 0.5),
             "p50_s": float(np.percentile(lat, 50)),
             "p99_s": float(np.percentile(lat, 99)),
             "mean_s": float(lat.mean()),

@@ -213,3 +213,33 @@ def test_tensor_engine_past_the_exact_row_limit(pkg, golden_cases, monkeypatch, 
                       use_generator_pruning=case["use_generator_pruning"], engine=engm.Engine(method="tensor"),
                       warn_complexity=False)
     assert digest_pairs(pkg.result_pairs(got, n_rows)) == case["digest"]
+
+
+def test_memory_guards_raise_instead_of_returning_a_partial_lattice(pkg):
+    """max_vram_gb / max_ram_gb below what the mine holds: MemoryError after the first counted level."""
+    syn = pkg.synthetic
+    t = syn.plain_small(n_rows=20_000, n_items=300, seed=5)
+    with pytest.raises(MemoryError, match="VRAM"):
+        pkg.apriori(table_of(t.indptr, t.items, t.n_rows), min_support=0.005, use_gpu=True, max_vram_gb=1e-9,
+                    warn_complexity=False)
+    with pytest.raises(MemoryError, match="RAM"):
+        pkg.apriori(table_of(t.indptr, t.items, t.n_rows), min_support=0.005, use_gpu=True, max_ram_gb=1e-9,
+                    warn_complexity=False)
+    got = pkg.apriori(table_of(t.indptr, t.items, t.n_rows), min_support=0.005, use_gpu=True, warn_complexity=False)
+    assert len(got) > 0
+
+
+def test_string_and_float_items_mine_like_their_integer_codes(pkg):
+    """Non-integer items: the same itemsets and supports as the integer ids they code to, with the items
+    themselves in the result (strings as strings, floats as float64)."""
+    syn = pkg.synthetic
+    t = syn.plain_small(n_rows=20_000, n_items=300, seed=5)
+    want = pkg.result_pairs(pkg.apriori(table_of(t.indptr, t.items, t.n_rows), min_support=0.005, use_gpu=True,
+                                        warn_complexity=False), t.n_rows)
+    names = np.array([f"item-{i:04d}" for i in range(int(t.items.max()) + 1)])
+    rows = [list(names[t.items[t.indptr[r]:t.indptr[r + 1]]]) for r in range(t.n_rows)]
+    got = pkg.result_pairs(pkg.apriori(rows, min_support=0.005, use_gpu=True, warn_complexity=False), t.n_rows)
+    assert sorted(got) == sorted((tuple(names[i] for i in s), c) for s, c in want)
+    floats = [[float(x) + 0.5 for x in t.items[t.indptr[r]:t.indptr[r + 1]]] for r in range(t.n_rows)]
+    got_f = pkg.result_pairs(pkg.apriori(floats, min_support=0.005, use_gpu=True, warn_complexity=False), t.n_rows)
+    assert sorted(got_f) == sorted((tuple(i + 0.5 for i in s), c) for s, c in want)

@@ -53,3 +53,30 @@ def test_parameter_checks_need_no_gpu(pkg, kw, exc, match):
     device work, with the reference's exception types."""
     with pytest.raises(exc, match=match):
         pkg.apriori([[1, 2], [2, 3]], use_gpu=True, **kw)
+
+
+def test_non_integer_items_are_coded_by_rank(pkg):
+    """Strings, floats and categorical values are coded to ranks among the distinct items (the reference's
+    _coded_items, core/apriori.py:277-284), nulls dropped; mixed kinds are refused."""
+    api = import_module(pkg.__name__ + ".api")
+    rows = [["milk", "bread"], None, ["eggs", None, "bread"], ["milk"]]
+    indptr, codes, _, labels = api._list_column(rows, "items")
+    assert list(labels) == ["bread", "eggs", "milk"]
+    assert indptr.tolist() == [0, 2, 2, 4, 5]
+    assert [labels[c] for c in codes] == ["milk", "bread", "eggs", "bread", "milk"]
+    indptr, codes, _, labels = api._list_column({"items": [[2.5, 1.0], [1.0]]}, "items")
+    assert labels.dtype == np.float64 and list(labels) == [1.0, 2.5] and codes.tolist() == [1, 0, 0]
+    indptr, ids, _, labels = api._list_column([[3, 1], [2]], "items")
+    assert labels is None and ids.tolist() == [3, 1, 2]
+    with pytest.raises(TypeError, match="must all be integers"):
+        api._list_column([[1, "a"]], "items")
+
+
+def test_categorical_pyarrow_items_come_back_as_strings(pkg):
+    pa = pytest.importorskip("pyarrow")
+    api = import_module(pkg.__name__ + ".api")
+    dict_type = pa.dictionary(pa.int32(), pa.string())
+    values = pa.array(["b", "a", "b", "c"]).cast(dict_type)
+    col = pa.LargeListArray.from_arrays(pa.array([0, 2, 4], pa.int64()), values)
+    indptr, codes, _, labels = api._list_column(pa.table({"items": col}), "items")
+    assert list(labels) == ["a", "b", "c"] and codes.tolist() == [1, 0, 1, 2]

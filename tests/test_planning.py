@@ -47,3 +47,16 @@ def test_row_wise_crossovers_are_the_reference_constants(engm):
     # gpu/row_split_chunks.py:124-159: K2_ROWS_MAX_R and K3_ROWS_MAX_R.
     assert engm.K2_ROWS_MAX_R == 3.95e-3
     assert engm.K3_ROWS_MAX_R == 2.5e-4
+
+
+def test_memory_guard_raises_past_either_limit(engm):
+    """The between-level guard (gpu/row_split.py:467-487): MemoryError naming the level and the limit."""
+    import pytest
+
+    engm.check_memory_guard(3, 10.0, 20.0, 800.0, 70.0)
+    engm.check_memory_guard(3, 10.0, 20.0, None, None)
+    with pytest.raises(MemoryError, match=r"after K=4: RAM=12.0GB exceeds max_ram_gb=8"):
+        engm.check_memory_guard(4, 12.0, 1.0, 8.0, 70.0)
+    with pytest.raises(MemoryError, match=r"after K=2: VRAM=71.0GB exceeds max_vram_gb=70.0GB.*INCOMPLETE"):
+        engm.check_memory_guard(2, 1.0, 71.0, 800.0, 70.0)
+    assert engm.host_rss_gb() > 0

@@ -40,6 +40,8 @@ def test_results_alone_equal_results_in_the_mix(pkg, served):
         mixed = [f.result(timeout=300) for f in futs]
         stats = server.stats()
     assert stats["requests"] == len(reqs) and stats["p99_s"] >= stats["p50_s"] > 0
+    # Requests on the same dataset with thresholds within 2x share one mine.
+    assert any(r.batch > 1 for r in mixed) and stats["mines"] < len(reqs)
     for (d, s, ml), res in zip(reqs, mixed):
         ds = datasets[d]
         alone = engm.Engine(chunk_cands=1 << 24, proj_bytes=1 << 30).mine(ds.bitvecs, ds.n_rows, s, ml)
@@ -80,3 +82,17 @@ def test_replay_reports_latency(pkg, served):
         st = server.stats()
     assert st["requests"] == 24
     assert st["p99_s"] >= st["p50_s"]
+
+
+def test_merged_and_unmerged_serving_agree(pkg, served):
+    """merge_ratio=1 (every request mined on its own) and the default merging give identical results."""
+    serve, _, datasets = served
+    reqs = [(1, s, ml) for s, ml in ((0.01, None), (0.012, 3), (0.015, 2), (0.02, None))]
+    out = {}
+    for ratio in (1.0, 4.0):
+        with serve.Server(datasets, slots=1, merge_ratio=ratio) as server:
+            futs = [server.submit(d, s, ml) for d, s, ml in reqs]
+            out[ratio] = [f.result(timeout=300) for f in futs]
+    assert all(r.batch == 1 for r in out[1.0])
+    for a, b in zip(out[1.0], out[4.0]):
+        assert _canon(a.levels) == _canon(b.levels)
