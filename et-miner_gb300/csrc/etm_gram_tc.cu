@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
     const int64_t* __restrict__ cld, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
     const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
     const uint8_t* __restrict__ cls, int32_t min_count, int32_t* __restrict__ out, uint32_t* __restrict__ surv,
-    unsigned long long* __restrict__ work_counter, uint64_t first_wait_ns) {
+    unsigned long long* __restrict__ work_counter, uint64_t first_wait_ns, bool blocked) {
     constexpr int T = Fmt<FMT>::T;
     constexpr int TH = T / 2;  // A rows per accumulator
     constexpr int WORDS = Fmt<FMT>::WORDS;
@@ -323,8 +323,11 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
         const int64_t n_stages = ceil_div<int64_t>(words, WORDS);
         if (tid < 256) {
             const int64_t ia = a0 + tid, ib = b0 + tid;
-            off_a[tid] = tid < T && ia < m ? cbase[wi] + ia * cld[wi] : -1;
-            off_b[tid] = tid < T && ib < m ? cbase[wi] + ib * cld[wi] : -1;
+            // Row-major rows: member i at cbase + i cld. Blocked rows (blocks of T members stored 4-word chunk
+            // by chunk, so a stage's words of one block are one run): member i at cbase + (i / T) T cld + 4 (i % T).
+            const int64_t cw = cld[wi];
+            off_a[tid] = tid < T && ia < m ? cbase[wi] + (blocked ? ua * T * cw + 4 * tid : ia * cw) : -1;
+            off_b[tid] = tid < T && ib < m ? cbase[wi] + (blocked ? ub * T * cw + 4 * tid : ib * cw) : -1;
         }
         int any = cls == nullptr;
         if (!any && tid < T) {
@@ -353,8 +356,9 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
                 for (int q = 0; q < BW; q += 2) {
                     const int64_t w = s0 * WORDS + q;
                     ulonglong2 v = make_ulonglong2(0, 0);
-                    if (off >= 0 && w + 1 < lim) v = __ldg(reinterpret_cast<const ulonglong2*>(src + off + w));
-                    else if (off >= 0 && w < lim) v.x = __ldg(src + off + w);
+                    const int64_t at = off + (blocked ? (w >> 2) * (4 * T) + (w & 3) : w);
+                    if (off >= 0 && w + 1 < lim) v = __ldg(reinterpret_cast<const ulonglong2*>(src + at));
+                    else if (off >= 0 && w < lim) v.x = __ldg(src + at);
                     x[q] = v.x;
                     x[q + 1] = v.y;
                 }
@@ -560,7 +564,7 @@ template <int FMT>
 int launch_gram(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                 const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
                 int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t min_count,
-                int32_t* out, uint32_t* surv, int64_t* work_counter, cudaStream_t s) {
+                int32_t* out, uint32_t* surv, int64_t* work_counter, bool blocked, cudaStream_t s) {
     static bool configured = false;
     uint64_t first_wait;
     {
@@ -577,7 +581,7 @@ int launch_gram(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cword
     gram_kernel<FMT><<<grid, THREADS, SMEM_BYTES, s>>>(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups,
                                                        work_off, n_work, chunk_base, cls, min_count, out, surv,
                                                        reinterpret_cast<unsigned long long*>(work_counter),
-                                                       first_wait);
+                                                       first_wait, blocked);
     ETM_LAUNCHED("gram_tc");
     return ETM_OK;
 }
@@ -587,7 +591,7 @@ int launch_gram(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cword
 namespace etm {
 
 int gram_block_members(int32_t elem) {
-    const int e = elem & ~ETM_TC_WIDE;
+    const int e = elem & ~(ETM_TC_WIDE | ETM_TC_BLOCKED);
     return e == ETM_TC_MXF4 ? Fmt<4>::T : e == 1 || e == 2 ? Fmt<1>::T : 0;
 }
 
@@ -595,11 +599,13 @@ int gram_tc(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, c
             const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
             int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t elem, int32_t min_count,
             int32_t* out, uint32_t* surv, int64_t* work_counter, cudaStream_t s) {
-    // elem: 1 = e4m3, 2 = f16, ETM_TC_MXF4 = packed e2m1; ETM_TC_WIDE is accepted and changes nothing.
-    const int e = elem & ~ETM_TC_WIDE;
+    // elem: 1 = e4m3, 2 = f16, ETM_TC_MXF4 = packed e2m1; ETM_TC_WIDE is accepted and changes nothing;
+    // + ETM_TC_BLOCKED: the member rows are in the projection's blocked layout with blocks of T members.
+    const bool blocked = (elem & ETM_TC_BLOCKED) != 0;
+    const int e = elem & ~(ETM_TC_WIDE | ETM_TC_BLOCKED);
     ETM_REQUIRE(e == 1 || e == 2 || e == ETM_TC_MXF4, ETM_EINVAL,
                 "gram_tc: element code %d (1 = e4m3, 2 = f16, %d = e2m1 block-scaled)", elem, ETM_TC_MXF4);
-#define ETM_GRAM_ARGS cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, n_tiles, chunk_base, cls, min_count, out, surv, work_counter, s
+#define ETM_GRAM_ARGS cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work, n_tiles, chunk_base, cls, min_count, out, surv, work_counter, blocked, s
     if (e == ETM_TC_MXF4) return launch_gram<4>(ETM_GRAM_ARGS);
     return e == 2 ? launch_gram<2>(ETM_GRAM_ARGS) : launch_gram<1>(ETM_GRAM_ARGS);
 #undef ETM_GRAM_ARGS

@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(PT) prefix_segments_kernel(const uint64_t* __r
             unsigned t = 0;
             for (int i = 0; i < P_WARPS; i++) t += part[i];
             so[s] = run;
-            run += (t + 63) / 64;
+            run += ((t + 63) / 64 + 3) & ~3u;  // whole 4-word chunks
         }
         __syncthreads();
     }
@@ -184,6 +184,17 @@ __global__ void __launch_bounds__(PT) prefix_segments_kernel(const uint64_t* __r
         out_words[wi] = run;
     }
 }
+
+// Projected member rows: row-major (blk = 0: word w of member j at j stride + w), or blocked (blk > 0: the
+// members in blocks of blk, each block stored chunk by chunk: 4-word chunk c of every member of the block,
+// then chunk c + 1; word w of member j at (j / blk) stride blk + (w / 4) 4 blk + (j % blk) 4 + w % 4), so
+// the tensor-core Gram's producers, one per member of a block, read a stage's words of consecutive members
+// as one contiguous run. Offsets are in words from the work entry's base.
+__host__ __device__ inline int64_t proj_member_offset(int64_t j, int64_t stride, int64_t blk) {
+    return blk > 0 ? (j / blk) * stride * blk + (j % blk) * 4 : j * stride;
+}
+// Offset of word w (a multiple of 4 under a blocked layout) within a member's row.
+__host__ __device__ inline int64_t proj_word_offset(int64_t w, int64_t blk) { return blk > 0 ? (w >> 2) * 4 * blk : w; }
 
 struct PassArgs {
     const uint64_t* fbv;
@@ -195,8 +206,9 @@ struct PassArgs {
     uint64_t* stage;
     const uint32_t* l32;
     int pass_rows, pass_words;
-    uint64_t* dst;
-    int64_t stride, out0;
+    uint64_t* dst;        // the work entry's projected rows (cbuf + cbase)
+    int64_t stride, out0; // words per member row; word of the row where this pass's words start
+    int64_t blk;          // members per layout block (0: row-major member rows)
     uint64_t* park;  // MPI x 4 MAX_CHUNKS words per warp of shared memory
     uint64_t* bars;  // two mbarriers (shared memory): group slots 0 and 1 of the stage buffers
     int32_t* ids;    // ID_RING member column ids (shared memory)
@@ -229,7 +241,9 @@ __device__ __forceinline__ bool gather_members(const PassArgs& a, uint32_t& phas
             rb[i] = r1 < a.pass_rows ? (l1 >> 5) << 2 : SEG_W * 8;
             ma[i] = 1u << (l0 & 31u);
             mb[i] = 1u << (l1 & 31u);
-            valid |= (t < a.pass_words ? 1u : 0u) << i;
+            // Every word of a chunk holding a word of the pass (the words past the pass are zero: pieces are
+            // padded to whole 4-word chunks).
+            valid |= ((warp + P_WARPS * k) < ((a.pass_words + 3) >> 2) ? 1u : 0u) << i;
         }
     }
     // Copies: members t MPI .. t MPI + MPI - 1 (group t) go to group slot t % 2 (stage buffers
@@ -264,7 +278,9 @@ __device__ __forceinline__ bool gather_members(const PassArgs& a, uint32_t& phas
     const uint8_t* sbytes = reinterpret_cast<const uint8_t*>(a.stage);
     uint64_t* park = a.park + warp * MPI * 4 * MAX_CHUNKS;
     const bool my_store = lane < 4 * MAX_CHUNKS && ((valid >> lane) & 1u);
-    uint64_t* out = a.dst + a.out0 + 4 * (warp + P_WARPS * (lane >> 2)) + (lane & 3);
+    // Lane l stores word (l & 3) of the pass's 4-word chunk warp + P_WARPS (l >> 2), for members j .. j + MPI - 1.
+    const int64_t wpos = a.out0 + 4 * (warp + P_WARPS * (lane >> 2));
+    uint64_t* out_w = a.dst + proj_word_offset(wpos, a.blk) + (lane & 3);
     for (int j0 = 0; j0 < m; j0 += NSTAGE) {
         // Unrolled over the stage buffers: members j0 + u .. j0 + u + MPI - 1 sit in buffers u ...
 #pragma unroll
@@ -312,9 +328,8 @@ __device__ __forceinline__ bool gather_members(const PassArgs& a, uint32_t& phas
             if (my_store) {
 #pragma unroll
                 for (int v = 0; v < MPI; v++)
-                    if (j + v < m) out[v * a.stride] = park[v * 4 * MAX_CHUNKS + lane];
+                    if (j + v < m) out_w[proj_member_offset(j + v, a.stride, a.blk)] = park[v * 4 * MAX_CHUNKS + lane];
             }
-            out += MPI * a.stride;
             __syncwarp();
         }
     }
@@ -335,7 +350,7 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
                                                          const int64_t* __restrict__ cld,
                                                          uint64_t* __restrict__ cbuf,
                                                          unsigned long long* __restrict__ work_counter,
-                                                         uint64_t first_wait_ns) {
+                                                         uint64_t first_wait_ns, int64_t blk) {
     extern __shared__ __align__(16) uint8_t psmem[];
     uint64_t* stage = reinterpret_cast<uint64_t*>(psmem);  // NSTAGE x (SEG_W member words + zero pad)
     uint64_t* pw = reinterpret_cast<uint64_t*>(psmem + NSTAGE * STAGE_BYTES);  // SEG_W prefix words
@@ -374,7 +389,7 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
         const int nw = (int)min64(SEG_W, n_words - w0);
         const int64_t* so = seg_off + wi * (n_seg + 1);
         const int64_t stride = cld[wi];
-        uint64_t* dst = cbuf + cbase[wi] + so[s];
+        uint64_t* dst = cbuf + cbase[wi];
         __syncthreads();  // the previous unit is done with the shared buffers
         if (threadIdx.x < plen) pref[threadIdx.x] = rows[first * width + threadIdx.x];
         __syncthreads();
@@ -418,7 +433,8 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
                 list[((x >> 6) << 6) + ((x & 31) << 1) + ((x >> 5) & 1)] = 0;
             __syncthreads();
             const PassArgs pa{fbv, ld, rows, width, first, m, w0, nw, stage, reinterpret_cast<const uint32_t*>(list),
-                              pass_rows, pass_words, dst, stride, p0 >> 6, park, bars, ids, first_wait_ns};
+                              pass_rows, pass_words, dst, stride, so[s] + (p0 >> 6), blk, park, bars, ids,
+                              first_wait_ns};
             if (!gather_members(pa, phase)) {
                 stop = true;
                 break;
@@ -430,10 +446,10 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
             // Zero the words after the last piece, up to the member stride.
             const int64_t used = so[n_seg];
             const int64_t pad = stride - used;
-            uint64_t* row0 = cbuf + cbase[wi] + used;
             for (int64_t idx = threadIdx.x; idx < m * pad; idx += PT) {
                 const int64_t j = idx / pad;
-                row0[j * stride + (idx - j * pad)] = 0ULL;
+                const int64_t w = used + (idx - j * pad);
+                dst[proj_member_offset(j, stride, blk) + proj_word_offset(w & ~3LL, blk) + (w & 3)] = 0ULL;
             }
         }
     }
@@ -502,10 +518,11 @@ extern "C" int etm_prefix_segments(const uint64_t* fbv, int64_t ld, int64_t n_wo
     return ETM_OK;
 }
 
-extern "C" int etm_project(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
-                           const int64_t* grp_first, const int32_t* grp_size, const int64_t* work_groups,
-                           int64_t n_work, const int64_t* seg_off, const int64_t* cbase, const int64_t* cld,
-                           uint64_t* cbuf, int64_t* work_counter, void* stream) {
+static int project_impl(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                        const int64_t* grp_first, const int32_t* grp_size, const int64_t* work_groups, int64_t n_work,
+                        const int64_t* seg_off, const int64_t* cbase, const int64_t* cld, uint64_t* cbuf,
+                        int64_t* work_counter, int64_t blk, void* stream) {
+    ETM_REQUIRE(blk >= 0 && blk <= 4096, ETM_EINVAL, "etm_project: blk %lld out of range (0..4096)", (long long)blk);
     ETM_REQUIRE(width >= 2 && width <= 64, ETM_EINVAL, "etm_project: width %d out of range (2..64)", width);
     ETM_REQUIRE(ld >= n_words && n_words >= 0 && ld % 2 == 0, ETM_EINVAL, "etm_project: ld must be even and >= n_words");
     ETM_REQUIRE((reinterpret_cast<uintptr_t>(fbv) & 15) == 0, ETM_EINVAL, "etm_project: fbv must be 16-byte aligned");
@@ -523,9 +540,27 @@ extern "C" int etm_project(const uint64_t* fbv, int64_t ld, int64_t n_words, con
                                                                    work_groups, n_work, n_seg, seg_off, cbase, cld,
                                                                    cbuf,
                                                                    reinterpret_cast<unsigned long long*>(work_counter),
-                                                                   g_proj_first_wait_ns.load());
+                                                                   g_proj_first_wait_ns.load(), blk);
     ETM_LAUNCHED("project");
     return ETM_OK;
+}
+
+extern "C" int etm_project(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                           const int64_t* grp_first, const int32_t* grp_size, const int64_t* work_groups,
+                           int64_t n_work, const int64_t* seg_off, const int64_t* cbase, const int64_t* cld,
+                           uint64_t* cbuf, int64_t* work_counter, void* stream) {
+    return project_impl(fbv, ld, n_words, rows, width, grp_first, grp_size, work_groups, n_work, seg_off, cbase, cld,
+                        cbuf, work_counter, 0, stream);
+}
+
+extern "C" int etm_project_blocked(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows,
+                                   int32_t width, const int64_t* grp_first, const int32_t* grp_size,
+                                   const int64_t* work_groups, int64_t n_work, const int64_t* seg_off,
+                                   const int64_t* cbase, const int64_t* cld, int64_t blk, uint64_t* cbuf,
+                                   int64_t* work_counter, void* stream) {
+    ETM_REQUIRE(blk >= 1, ETM_EINVAL, "etm_project_blocked: blk must be >= 1");
+    return project_impl(fbv, ld, n_words, rows, width, grp_first, grp_size, work_groups, n_work, seg_off, cbase, cld,
+                        cbuf, work_counter, blk, stream);
 }
 
 extern "C" int etm_count_tiles_proj(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords,

@@ -75,14 +75,16 @@ def mining_min_count(min_support: float, n_rows: int) -> int:
 
 
 def proj_stride(pcnt: np.ndarray, n_words: int) -> np.ndarray:
-    """Words per member of a projected group: its prefix rows in whole words, one padded word per
-    segment of PROJ_SEG_WORDS bitvector words, rounded up to 32 (at least 32)."""
+    """Words per member of a projected group: its prefix rows in whole words, plus up to four padded words
+    per segment of PROJ_SEG_WORDS bitvector words (each segment's piece ends on a 4-word chunk), rounded up
+    to 32 (at least 32)."""
     n_seg = max(1, -(-int(n_words) // PROJ_SEG_WORDS))
-    return np.maximum(32, ((np.asarray(pcnt, np.int64) + 63) // 64 + n_seg + 31) // 32 * 32)
+    return np.maximum(32, ((np.asarray(pcnt, np.int64) + 63) // 64 + 4 * n_seg + 31) // 32 * 32)
 
 
 TC_MXF4 = 4  # ETM_TC_MXF4: packed e2m1 operands under kind::mxf4 (tc_elem code)
 TC_WIDE = 16  # ETM_TC_WIDE: accepted in tc_elem and ignored (every code runs the block-pair kernel)
+TC_BLOCKED = 32  # ETM_TC_BLOCKED: the Gram reads member rows in the projection's blocked layout
 #: Packed e2m1 operands: the fastest exact form measured on GB300 (0.86 s per dense K=2 mine against 1.11 s
 #: with e4m3 operands).
 DEFAULT_TC_ELEM = TC_MXF4
@@ -436,14 +438,17 @@ class Engine:
         cnt = pcnt[gids]
         n_seg = max(1, -(-n_words // PROJ_SEG_WORDS))
         cl = proj_stride(cnt, n_words)
+        # The Gram reads blocked rows (blocks of its block size, chunk by chunk); rows past m are not written.
+        blk = tc_block(self.tc_elem) if method == 1 else 0
+        m_rows = -(-m // blk) * blk if blk else m
         cb = np.zeros(len(gids) + 1, np.int64)
-        np.cumsum(m * cl, out=cb[1:])
+        np.cumsum(m_rows * cl, out=cb[1:])
         toff = np.zeros(len(gids) + 1, np.int64)
         np.cumsum(_tile_items(m, method, self.tc_elem), out=toff[1:])
         n = len(gids)
         # cwords starts as the bound (whole words of the prefix rows plus one padded word per segment);
         # etm_prefix_segments overwrites it with the exact padded length.
-        host = np.concatenate([gids.astype(np.int64), toff, cb[:-1], (cnt + 63) // 64 + n_seg, cl])
+        host = np.concatenate([gids.astype(np.int64), toff, cb[:-1], (cnt + 63) // 64 + 4 * n_seg, cl])
         d = torch.from_numpy(host).to(self.device)
         wg, wo = d[:n], d[n:2 * n + 1]
         cbase, cwords, cld = d[2 * n + 1:3 * n + 1], d[3 * n + 1:4 * n + 1], d[4 * n + 1:5 * n + 1]
@@ -457,13 +462,17 @@ class Engine:
         check(st, "etm_prefix_segments")
         # Algorithmic bytes: every member's column words and the prefix words read once, the strides written.
         st = self._launch("project", int(((m + width - 1) * n_words).sum() * 8 + (m * cl).sum() * 8),
-                          lambda: self.lib.etm_project(_p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first),
-                                                       _p(grp_size), _p(wg), n, _p(seg_off), _p(cbase), _p(cld),
-                                                       _p(cbuf), _p(proj_counter), _stream()))
+                          lambda: self.lib.etm_project_blocked(
+                              _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(wg), n,
+                              _p(seg_off), _p(cbase), _p(cld), blk, _p(cbuf), _p(proj_counter), _stream())
+                          if blk else self.lib.etm_project(
+                              _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(wg), n,
+                              _p(seg_off), _p(cbase), _p(cld), _p(cbuf), _p(proj_counter), _stream()))
         check(st, "etm_project")
         self._waits_pending = True
         self.launches += 2
         return dict(d=d, cbuf=cbuf, cbase=cbase, cwords=cwords, cld=cld, wg=wg, wo=wo, n=n, n_tiles=int(toff[-1]),
+                    blocked=bool(blk),
                     nbytes=int((m * ((cnt + 63) // 64)).sum() * 8),
                     macs=float((m * (m - 1) / 2 * cnt.astype(np.float64)).sum()))
 
@@ -472,7 +481,7 @@ class Engine:
         prep["d"].record_stream(torch.cuda.current_stream())
         self._count_words(prep["cbuf"], prep["cbase"], prep["cwords"], prep["cld"], grp_size, cand_off, prep["wg"],
                           prep["wo"], prep["n"], prep["n_tiles"], base, cls, counts, method, prep["nbytes"],
-                          prep["macs"], sel)
+                          prep["macs"], sel, prep["blocked"])
 
     def _count_projected(self, fbv, ldp, n_words, gen, grp_first, grp_size, cand_off, gids, sizes, pcnt, base, cls,
                          counts, method, sel=None):
@@ -481,12 +490,14 @@ class Engine:
         self._count_prepped(prep, grp_size, cand_off, base, cls, counts, method, sel)
 
     def _count_words(self, cbuf, cbase, cwords, cld, grp_size, cand_off, wg, wo, n, n_tiles, base, cls, counts,
-                     method, nbytes, macs, sel=None):
+                     method, nbytes, macs, sel=None, blocked: bool = False):
         """Tile-pair counts over member words laid out as cbuf[cbase[wi] + i * cld[wi]]: tensor or popcount.
 
         ``macs`` is the useful work: one multiply-add per candidate pair and row (sum of C(m,2) x rows).
-        ``sel`` = (min_count, survivor bitmask) selects the fused-threshold form.
+        ``sel`` = (min_count, survivor bitmask) selects the fused-threshold form; ``blocked``: the rows are in
+        the projection's blocked layout (tensor method).
         """
+        elem = self.tc_elem | (TC_BLOCKED if blocked else 0)
         if method == 1:
             # The work counter lets the Gram's CTAs claim block pairs dynamically (one per engine: the Gram
             # launches of an engine run in turn on its main stream).
@@ -494,11 +505,11 @@ class Engine:
             if sel is None:
                 fn = lambda: self.lib.etm_count_tiles_tc(  # noqa: E731
                     _p(cbuf), _p(cbase), _p(cwords), _p(cld), _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, n_tiles,
-                    base, _p(cls), self.tc_elem, _p(counts), _p(counter), _stream())
+                    base, _p(cls), elem, _p(counts), _p(counter), _stream())
             else:
                 fn = lambda: self.lib.etm_count_tiles_tc_sel(  # noqa: E731
                     _p(cbuf), _p(cbase), _p(cwords), _p(cld), _p(grp_size), _p(cand_off), _p(wg), _p(wo), n, n_tiles,
-                    base, _p(cls), self.tc_elem, sel[0], _p(counts), _p(sel[1]), _p(counter), _stream())
+                    base, _p(cls), elem, sel[0], _p(counts), _p(sel[1]), _p(counter), _stream())
             check(self._launch("gram_tc", nbytes, fn, flops=2 * macs), "etm_count_tiles_tc")
             self.used_tensor = True
             self._waits_pending = True
@@ -610,7 +621,8 @@ class Engine:
             else:
                 proj = big & (pcnt < self.proj_density * n_rows)
         pwords = proj_stride(pcnt, n_words)
-        pbytes = np.where(proj, sizes * pwords * 8, 0)
+        blk = tc_block(self.tc_elem) if tensor else 0
+        pbytes = np.where(proj, (-(-sizes // blk) * blk if blk else sizes) * pwords * 8, 0)
         pcum = np.zeros(G + 1, np.int64)
         np.cumsum(pbytes, out=pcum[1:])
         cap = int(min(total, max(1 << 16, 2 * gen.n)))

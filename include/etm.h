@@ -59,6 +59,9 @@ extern "C" {
 #define ETM_TC_MXF4 4
 /* Accepted in elem for compatibility and ignored: every element code runs the block-pair kernel. */
 #define ETM_TC_WIDE 16
+/* Added to elem: the member rows are in the blocked layout etm_project_blocked writes, with blocks of
+ * etm_gram_block_members(elem) members (cbase of each work entry at a block-aligned member 0). */
+#define ETM_TC_BLOCKED 32
 
 /* Rows of one projection segment: 1024 bitvector words (65,536 transactions). */
 #define ETM_PROJ_SEG_WORDS 1024
@@ -221,10 +224,11 @@ int etm_triple_counts_rows(const int64_t* row_ptr, const int32_t* cols, int64_t 
  *                      ETM_PROJ_SEG_WORDS words: seg_off int64 [n_work][n_seg+1]
  *                      (n_seg = ceil(n_words / ETM_PROJ_SEG_WORDS)) = the word
  *                      offset of each segment's piece of a projected row, each
- *                      piece ceil(count / 64) words; out_words[wi] = the total;
+ *                      piece ceil(count / 64) words rounded up to a multiple of
+ *                      4 (whole 32-byte chunks); out_words[wi] = the total;
  *   etm_project        member i of group wi -> cbuf[cbase[wi] + i*cld[wi] ...]:
  *                      per segment, its column's bits at the segment's prefix
- *                      rows, 64 per word, the piece zero-padded to whole words
+ *                      rows, 64 per word, the piece zero-padded to whole chunks
  *                      at seg_off; zero from out_words[wi] up to cld[wi] words
  *                      (cld % 32 == 0, cbase even, ld even, fbv 16-byte aligned).
  *                      Padding rows are zero in every member, so pair counts
@@ -248,6 +252,21 @@ int etm_project(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t*
                 const int64_t* grp_first, const int32_t* grp_size, const int64_t* work_groups, int64_t n_work,
                 const int64_t* seg_off, const int64_t* cbase, const int64_t* cld, uint64_t* cbuf,
                 int64_t* work_counter, void* stream);
+/*
+ * etm_project writing the blocked layout: the members of each work entry in
+ * blocks of blk (1..4096), each block stored 4-word chunk by chunk, so word w
+ * of member j sits at cbase + (j / blk) * cld * blk + (w / 4) * 4 * blk +
+ * (j % blk) * 4 + w % 4. The tensor-core Gram's producers (one per member of
+ * a block) then read each stage's words of a block as one contiguous run
+ * (elem | ETM_TC_BLOCKED, blk = etm_gram_block_members(elem)). Each work
+ * entry needs ceil(m / blk) * blk * cld words (rows past m are never read).
+ * New in this engine, like the projection itself.
+ */
+int etm_project_blocked(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                        const int64_t* grp_first, const int32_t* grp_size, const int64_t* work_groups, int64_t n_work,
+                        const int64_t* seg_off, const int64_t* cbase, const int64_t* cld, int64_t blk, uint64_t* cbuf,
+                        int64_t* work_counter, void* stream);
+
 int etm_count_tiles_proj(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                          const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
                          const int64_t* work_off, int64_t n_work, int64_t chunk_base, const uint8_t* cls,

@@ -324,7 +324,7 @@ def test_pair_counts_rows_match_host(pkg, lib, max_len):
 
 def _projection_reference(bits, ld, n_words, groups, stride):
     """Per group (prefix columns, member columns): each member's bits at the prefix rows, per segment of
-    ETM_PROJ_SEG_WORDS words, every segment's piece padded to whole 64-bit words, zeros to the stride."""
+    ETM_PROJ_SEG_WORDS words, every segment's piece padded to whole 4-word chunks, zeros to the stride."""
     seg = 1024
     out = []
     for (prefix, members), cl in zip(groups, stride):
@@ -337,7 +337,7 @@ def _projection_reference(bits, ld, n_words, groups, stride):
             for s0 in range(0, n_words * 64, seg * 64):
                 sel = bits[m][s0:s0 + seg * 64][mask[s0:s0 + seg * 64]]
                 if len(sel):
-                    pad = np.zeros((len(sel) + 63) // 64 * 64, np.uint8)
+                    pad = np.zeros((len(sel) + 255) // 256 * 256, np.uint8)
                     pad[:len(sel)] = sel
                     words.append(np.packbits(pad, bitorder="little").view(np.uint64))
             w = np.concatenate(words) if words else np.zeros(0, np.uint64)
@@ -348,10 +348,12 @@ def _projection_reference(bits, ld, n_words, groups, stride):
     return out
 
 
+@pytest.mark.parametrize("blk", [0, 3, 240])
 @pytest.mark.parametrize("n_words,width", [(1, 2), (1023, 2), (1024, 3), (1025, 2), (3001, 3), (2500, 2)])
-def test_segmented_projection(pkg, lib, n_words, width):
-    """etm_prefix_segments + etm_project against the host restatement, including a dense prefix (more
-    prefix rows in a segment than one pass lists), an empty prefix and the zero padding."""
+def test_segmented_projection(pkg, lib, n_words, width, blk):
+    """etm_prefix_segments + etm_project (row-major) or etm_project_blocked (blocks of blk members, chunk by
+    chunk) against the host restatement, including a dense prefix (more prefix rows in a segment than one
+    pass lists), an empty prefix and the zero padding."""
     import importlib
 
     import torch
@@ -388,8 +390,9 @@ def test_segmented_projection(pkg, lib, n_words, width):
     cnt = np.array(cnt, np.int64)
     cl = eng.proj_stride(cnt, n_words)
     m = sizes[wg].astype(np.int64)
+    m_rows = -(-m // blk) * blk if blk else m
     cb = np.zeros(len(wg) + 1, np.int64)
-    np.cumsum(m * cl, out=cb[1:])
+    np.cumsum(m_rows * cl, out=cb[1:])
     n_seg = -(-n_words // 1024)
     d_fbv, d_rows = _dev(fbv_h.view(np.int64)), _dev(rows)
     d_first, d_size, d_wg = _dev(first), _dev(sizes), _dev(wg)
@@ -403,9 +406,14 @@ def test_segmented_projection(pkg, lib, n_words, width):
     ctr = torch.zeros(1, dtype=torch.int64, device="cuda")  # held for the call
     counter = ctr.data_ptr() if n_words % 2 else None
     d_cbase, d_cld = _dev(cb[:-1].copy()), _dev(cl)
-    st = lib.etm_project(d_fbv.data_ptr(), ld, n_words, d_rows.data_ptr(), width, d_first.data_ptr(),
-                         d_size.data_ptr(), d_wg.data_ptr(), len(wg), seg_off.data_ptr(), d_cbase.data_ptr(),
-                         d_cld.data_ptr(), cbuf.data_ptr(), counter, _stream())
+    if blk:
+        st = lib.etm_project_blocked(d_fbv.data_ptr(), ld, n_words, d_rows.data_ptr(), width, d_first.data_ptr(),
+                                     d_size.data_ptr(), d_wg.data_ptr(), len(wg), seg_off.data_ptr(),
+                                     d_cbase.data_ptr(), d_cld.data_ptr(), blk, cbuf.data_ptr(), counter, _stream())
+    else:
+        st = lib.etm_project(d_fbv.data_ptr(), ld, n_words, d_rows.data_ptr(), width, d_first.data_ptr(),
+                             d_size.data_ptr(), d_wg.data_ptr(), len(wg), seg_off.data_ptr(), d_cbase.data_ptr(),
+                             d_cld.data_ptr(), cbuf.data_ptr(), counter, _stream())
     assert st == 0, lib.etm_last_error()
     got = cbuf.cpu().numpy().view(np.uint64)
     want = _projection_reference(bits.astype(bool), ld, n_words, [groups[g] for g in wg], cl)
@@ -414,10 +422,17 @@ def test_segmented_projection(pkg, lib, n_words, width):
     for k in range(len(wg)):
         seg_counts = [int(((np.logical_and.reduce([bits[c].astype(bool) for c in groups[wg[k]][0]]))
                            [s * 65536:(s + 1) * 65536]).sum()) for s in range(n_seg)]
-        expect_off = np.concatenate([[0], np.cumsum([(c + 63) // 64 for c in seg_counts])])
+        expect_off = np.concatenate([[0], np.cumsum([((c + 63) // 64 + 3) // 4 * 4 for c in seg_counts])])
         assert np.array_equal(so[k], expect_off)
         assert ow[k] == expect_off[-1] <= cl[k]
-        block = got[cb[k]:cb[k + 1]].reshape(m[k], cl[k])
+        if blk:
+            # Word w of member j at (j // blk) cl blk + (w // 4) 4 blk + (j % blk) 4 + w % 4.
+            j = np.arange(m[k])[:, None]
+            w = np.arange(cl[k])[None, :]
+            idx = (j // blk) * cl[k] * blk + (w // 4) * 4 * blk + (j % blk) * 4 + w % 4
+            block = got[cb[k]:cb[k + 1]][idx]
+        else:
+            block = got[cb[k]:cb[k + 1]].reshape(m[k], cl[k])
         assert np.array_equal(block, want[k]), f"work entry {k} (group {wg[k]})"
 
 

@@ -15,11 +15,12 @@ def engm(pkg):
 
 
 def _padded_words(prefix_rows: np.ndarray, n_words: int, seg: int) -> int:
-    """Words of a projected row: per segment of ``seg`` bitvector words, its prefix rows in whole words."""
+    """Words of a projected row: per segment of ``seg`` bitvector words, its prefix rows in whole words,
+    padded to whole 4-word chunks."""
     n = 0
     for s0 in range(0, n_words * 64, seg * 64):
         c = int(((prefix_rows >= s0) & (prefix_rows < s0 + seg * 64)).sum())
-        n += (c + 63) // 64
+        n += ((c + 63) // 64 + 3) // 4 * 4
     return n
 
 

@@ -114,9 +114,10 @@ def test_dense_bernoulli_tensor_matches_popcount(pkg):
         assert np.array_equal(ra, rb) and np.array_equal(ca, cb)
 
 
-def _gram_groups(lib, elem, seed=11):
+def _gram_groups(lib, elem, seed=11, blocked=False):
     """Member words of several groups of different sizes and lengths on the device, laid out as the
-    projection lays them out, with their host Gram (upper triangles, candidate order) and work lists."""
+    projection lays them out (row-major, or blocked in blocks of the kernel's block size), with their host
+    Gram (upper triangles, candidate order) and work lists."""
     import torch
 
     t = lib.etm_gram_block_members(elem)
@@ -124,15 +125,21 @@ def _gram_groups(lib, elem, seed=11):
     sizes = np.array([300, 1, 2, 257, 513, 40, 481], np.int64)
     cw = np.array([64, 2, 3, 130, 17, 1, 5], np.int64)  # words per member row (odd counts end in a part stage)
     cld = (cw + 31) // 32 * 32
+    rows_alloc = -(-sizes // t) * t if blocked else sizes
     cbase = np.zeros(len(sizes), np.int64)
-    cbase[1:] = np.cumsum(sizes * cld)[:-1]
-    buf = np.zeros(int((sizes * cld).sum()), np.uint64)
+    cbase[1:] = np.cumsum(rows_alloc * cld)[:-1]
+    buf = np.zeros(int((rows_alloc * cld).sum()), np.uint64)
     want = []
     for g in range(len(sizes)):
         m, w = int(sizes[g]), int(cw[g])
         x = rng.integers(0, 2**63, size=(m, w), dtype=np.int64).view(np.uint64)
         x &= rng.integers(0, 2**63, size=(m, w), dtype=np.int64).view(np.uint64)
-        buf[cbase[g]:cbase[g] + m * cld[g]].reshape(m, cld[g])[:, :w] = x
+        if blocked:
+            j = np.arange(m)[:, None]
+            ww = np.arange(w)[None, :]
+            buf[cbase[g] + (j // t) * cld[g] * t + (ww // 4) * 4 * t + (j % t) * 4 + ww % 4] = x
+        else:
+            buf[cbase[g]:cbase[g] + m * cld[g]].reshape(m, cld[g])[:, :w] = x
         bits = np.unpackbits(x.view(np.uint8), axis=1).astype(np.int64)
         want.append((bits @ bits.T)[np.triu_indices(m, 1)])
     want = np.concatenate(want).astype(np.int32)
@@ -152,19 +159,22 @@ def _gram_args(d):
             d["size"].data_ptr(), d["cand_off"].data_ptr(), d["wg"].data_ptr(), d["wo"].data_ptr())
 
 
+@pytest.mark.parametrize("blocked", [False, True])
 @pytest.mark.parametrize("elem", [1 | 16, 2, 4])
 @pytest.mark.parametrize("with_counter", [True, False])
-def test_wide_kernel_claimed_and_round_robin_items_agree(pkg, with_counter, elem):
-    """etm_count_tiles_tc over several groups of different sizes and lengths: block pairs claimed from a
-    work counter or taken round-robin give the same counts, equal to a host Gram."""
+def test_wide_kernel_claimed_and_round_robin_items_agree(pkg, with_counter, elem, blocked):
+    """etm_count_tiles_tc over several groups of different sizes and lengths, row-major or blocked member
+    rows: block pairs claimed from a work counter or taken round-robin give the same counts, equal to a host
+    Gram."""
     import torch
 
     lib = pkg.load_library()
-    t, d, want, n_work, n_items = _gram_groups(lib, elem)
+    t, d, want, n_work, n_items = _gram_groups(lib, elem, blocked=blocked)
     assert t == (240 if elem == 4 else 256)
     out = torch.full((len(want),), -7, dtype=torch.int32, device="cuda")
     counter = torch.full((1,), 12345, dtype=torch.int64, device="cuda")  # zeroed by the call
-    st = lib.etm_count_tiles_tc(*_gram_args(d), n_work, n_items, 0, None, elem, out.data_ptr(),
+    code = elem | (32 if blocked else 0)
+    st = lib.etm_count_tiles_tc(*_gram_args(d), n_work, n_items, 0, None, code, out.data_ptr(),
                                 counter.data_ptr() if with_counter else None, torch.cuda.current_stream().cuda_stream)
     assert st == 0, lib.etm_last_error()
     assert np.array_equal(out.cpu().numpy(), want)
