@@ -103,6 +103,7 @@ constexpr int ID_RING = 512;           // member column ids held in shared memor
 constexpr int MAX_CHUNKS = (LIST_CAP / 64 / 4 + (PT / 32) - 1) / (PT / 32);
 constexpr int P_WARPS = PT / 32;
 constexpr int PROJ_SMEM = STAGE_BYTES * NSTAGE + SEG_W * 8 + LIST_CAP * 2;
+static_assert(MPI == 4 && MAX_CHUNKS % 2 == 0, "the blocked store maps a warp onto 4 members x 2 chunks");
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 // Bulk (TMA) copies of whole member segments into shared memory, completed on an mbarrier.
@@ -325,10 +326,27 @@ __device__ __forceinline__ bool gather_members(const PassArgs& a, uint32_t& phas
                 }
             }
             __syncwarp();
-            if (my_store) {
+            if (a.blk == 0) {
+                if (my_store) {
 #pragma unroll
-                for (int v = 0; v < MPI; v++)
-                    if (j + v < m) out_w[proj_member_offset(j + v, a.stride, a.blk)] = park[v * 4 * MAX_CHUNKS + lane];
+                    for (int v = 0; v < MPI; v++)
+                        if (j + v < m) out_w[(int64_t)(j + v) * a.stride] = park[v * 4 * MAX_CHUNKS + lane];
+                }
+            } else {
+                // Blocked rows: the same chunk of consecutive members is contiguous, so lane l stores word l % 4
+                // of chunk kk + l / 16 for member j + (l / 4) % 4: two full 128-byte runs per store.
+                const uint32_t bk = (uint32_t)a.blk;
+                const int v = (lane >> 2) & 3;
+                uint32_t q = (uint32_t)(j + v) / bk, r = (uint32_t)(j + v) - q * bk;
+                const int64_t moff = (int64_t)q * a.stride * bk + 4 * (int64_t)r;
+#pragma unroll
+                for (int kk = 0; kk < MAX_CHUNKS; kk += 2) {
+                    const int k = kk + (lane >> 4);
+                    const int i = 4 * k + (lane & 3);
+                    if (k < MAX_CHUNKS && ((valid >> i) & 1u) && j + v < m)
+                        a.dst[moff + proj_word_offset(a.out0 + 4 * (warp + P_WARPS * k), a.blk) + (lane & 3)] =
+                            park[v * 4 * MAX_CHUNKS + i];
+                }
             }
             __syncwarp();
         }
