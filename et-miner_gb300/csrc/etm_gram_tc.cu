@@ -54,6 +54,7 @@
 // block raises an abort flag, every thread leaves its loop, the MMA thread
 // waits (bounded) for its issued MMAs, TMEM is freed, and the kernel records
 // ETM_ETIMEOUT in its status word instead of hanging.
+#include <cstdlib>
 #include <mutex>
 
 #include "etm_count.cuh"
@@ -69,6 +70,18 @@ constexpr int STAGES = 3;
 constexpr int HALF_BYTES = 128 * 128;          // one 128-row operand tile of 128-byte rows
 constexpr int SLOT_BYTES = 4 * HALF_BYTES;     // A (two 128-row halves), then B (256 rows)
 constexpr int SMEM_BYTES = STAGES * SLOT_BYTES + 1024;
+// Staged form (packed e2m1 over blocked rows): a loader warp copies each stage's raw bits (the block's
+// 32-byte chunk of every member: T x 32 bytes per block, one contiguous run in the blocked layout) into a
+// ring of RAW_STAGES shared-memory slots with bulk copies; the producers expand from there. Two operand
+// stages leave room for the ring.
+constexpr int ST_OPS = 2;
+constexpr int RAW_STAGES = 5;
+constexpr int RAW_BLOCK = 240 * 32;             // one block's raw chunk: 240 members x 32 bytes
+constexpr int RAW_SLOT = 2 * RAW_BLOCK;         // A block, then B block
+constexpr int ST_THREADS = PRODUCERS + 64;      // producers, the MMA warp, the loader warp
+constexpr int LOAD_WARP = MMA_WARP + 1;
+constexpr int ST_SMEM = ST_OPS * SLOT_BYTES + RAW_STAGES * RAW_SLOT + 1024;
+static_assert(ST_SMEM <= 227 * 1024 - 8192, "staged shared memory");
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t SF_COL = 480;               // FMT 4: scale factors in TMEM columns 480-511
 constexpr uint64_t WAIT_NS = 2000000000ull;    // every bounded wait: 2 s
@@ -198,6 +211,18 @@ __device__ __forceinline__ void mma_ss(uint32_t tmem_d, uint64_t a, uint64_t b, 
     }
 }
 
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Bulk (TMA) copy of `bytes` (a multiple of 16, both addresses 16-byte aligned) from global to shared memory,
+// completed on `bar` (complete_tx).
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                  : "memory");
@@ -231,8 +256,8 @@ __device__ __forceinline__ void store_row(uint8_t* tile, int r, const uint64_t* 
     }
 }
 
-template <int FMT>
-__global__ void __launch_bounds__(THREADS, 1) gram_kernel(
+template <int FMT, bool STAGED>
+__global__ void __launch_bounds__(STAGED ? ST_THREADS : THREADS, 1) gram_kernel(
     const uint64_t* __restrict__ src, const int64_t* __restrict__ cbase, const int64_t* __restrict__ cwords,
     const int64_t* __restrict__ cld, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
     const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
@@ -243,9 +268,13 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
     constexpr int WORDS = Fmt<FMT>::WORDS;
     constexpr int PF = Fmt<FMT>::PF;
     constexpr int BW = PF * WORDS;
+    constexpr int NST = STAGED ? ST_OPS : STAGES;  // operand stages
+    static_assert(!STAGED || (FMT == 4 && T * 32 == RAW_BLOCK), "the staged form serves packed e2m1 operands");
     extern __shared__ uint8_t dsmem[];
-    __shared__ __align__(8) uint64_t full_bar[STAGES];
-    __shared__ __align__(8) uint64_t empty_bar[STAGES];
+    __shared__ __align__(8) uint64_t full_bar[NST];
+    __shared__ __align__(8) uint64_t empty_bar[NST];
+    __shared__ __align__(8) uint64_t raw_full[STAGED ? RAW_STAGES : 1];
+    __shared__ __align__(8) uint64_t raw_empty[STAGED ? RAW_STAGES : 1];
     __shared__ __align__(8) uint64_t acc_bar;
     __shared__ __align__(8) uint64_t drain_bar;
     __shared__ uint32_t tmem_sh;
@@ -255,13 +284,20 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
     __shared__ int64_t next_sh;
 
     uint8_t* slots = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~uintptr_t(1023));
+    uint8_t* raw = slots + NST * SLOT_BYTES;  // staged form: RAW_STAGES slots of RAW_SLOT bytes
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
 
     if (tid == 0) {
-        for (int s = 0; s < STAGES; s++) {
+        for (int s = 0; s < NST; s++) {
             mbar_init(&full_bar[s], PRODUCERS);
             mbar_init(&empty_bar[s], 1);
+        }
+        if constexpr (STAGED) {
+            for (int s = 0; s < RAW_STAGES; s++) {
+                mbar_init(&raw_full[s], 1);
+                mbar_init(&raw_empty[s], PRODUCERS);
+            }
         }
         mbar_init(&acc_bar, 1);
         mbar_init(&drain_bar, 1);
@@ -298,6 +334,7 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
 
     const int64_t total = work_off[n_work];
     int64_t gstage = 0;
+    int64_t raw_issued = 0;  // loader: stages whose raw copies were issued
     uint32_t tile_iter = 0;
     // Block pairs in work-list order; with a work counter each CTA takes the next unclaimed one
     // (dynamic balance across groups of different lengths), else every gridDim.x-th.
@@ -348,40 +385,71 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
             // B row r: row r of the 256-row B tile; A row r: row r % TH of A half r / TH.
             const int dst = is_b ? 2 * HALF_BYTES : (prow / TH) * HALF_BYTES;
             const int hrow = is_b ? prow : prow % TH;
-            uint64_t cur[BW], nxt[BW];
-            // Words past the row's last stage are not read (they may lie past the buffer).
-            const int64_t lim = n_stages * WORDS;
-            auto load_batch = [&](int64_t s0, uint64_t* x) {
-#pragma unroll
-                for (int q = 0; q < BW; q += 2) {
-                    const int64_t w = s0 * WORDS + q;
-                    ulonglong2 v = make_ulonglong2(0, 0);
-                    const int64_t at = off + (blocked ? (w >> 2) * (4 * T) + (w & 3) : w);
-                    if (off >= 0 && w + 1 < lim) v = __ldg(reinterpret_cast<const ulonglong2*>(src + at));
-                    else if (off >= 0 && w < lim) v.x = __ldg(src + at);
-                    x[q] = v.x;
-                    x[q + 1] = v.y;
-                }
-            };
-            if (n_stages > 0) load_batch(0, cur);
-            for (int64_t s0 = 0; s0 < n_stages && !*abort_flag; s0 += PF) {
-                if (s0 + PF < n_stages) load_batch(s0 + PF, nxt);
-#pragma unroll
-                for (int j = 0; j < PF; j++) {
-                    const int64_t s = s0 + j;
-                    if (s >= n_stages) break;
+            if constexpr (STAGED) {
+                // Raw bits from the loader's ring (A block at 0, B block at RAW_BLOCK of a slot): wait for the
+                // slot, read this row's 32 bytes, release the slot, then expand into the operand stage.
+                const bool skip = idle || (is_b ? b0 : a0) + prow >= m;
+                const int raw_off = (is_b ? RAW_BLOCK : 0) + prow * 32;
+                for (int64_t s = 0; s < n_stages; s++) {
                     const int64_t G = gstage + s;
-                    const int slot = (int)(G % STAGES);
-                    const uint32_t use = (uint32_t)(G / STAGES);
-                    if (!mbar_wait(&empty_bar[slot], (use & 1u) ^ 1u, abort_flag, WAIT_NS)) break;
-                    if (off >= 0) {
-                        store_row<FMT>(slots + slot * SLOT_BYTES + dst, hrow, cur + j * WORDS);
+                    const int rs = (int)(G % RAW_STAGES);
+                    const uint32_t ruse = (uint32_t)(G / RAW_STAGES);
+                    const int os = (int)(G % NST);
+                    const uint32_t ouse = (uint32_t)(G / NST);
+                    if (!mbar_wait(&raw_full[rs], ruse & 1u, abort_flag, WAIT_NS)) break;
+                    uint64_t x[4] = {0, 0, 0, 0};
+                    if (!skip) {
+                        const uint4* r = reinterpret_cast<const uint4*>(raw + rs * RAW_SLOT + raw_off);
+                        const uint4 v0 = r[0], v1 = r[1];
+                        x[0] = (uint64_t)v0.x | ((uint64_t)v0.y << 32);
+                        x[1] = (uint64_t)v0.z | ((uint64_t)v0.w << 32);
+                        x[2] = (uint64_t)v1.x | ((uint64_t)v1.y << 32);
+                        x[3] = (uint64_t)v1.z | ((uint64_t)v1.w << 32);
+                    }
+                    mbar_arrive(&raw_empty[rs]);
+                    if (!mbar_wait(&empty_bar[os], (ouse & 1u) ^ 1u, abort_flag, WAIT_NS)) break;
+                    if (!skip) {
+                        store_row<FMT>(slots + os * SLOT_BYTES + dst, hrow, x);
                         fence_proxy_async();
                     }
-                    mbar_arrive(&full_bar[slot]);
+                    mbar_arrive(&full_bar[os]);
                 }
-#pragma unroll
-                for (int q = 0; q < BW; q++) cur[q] = nxt[q];
+            } else {
+                uint64_t cur[BW], nxt[BW];
+                // Words past the row's last stage are not read (they may lie past the buffer).
+                const int64_t lim = n_stages * WORDS;
+                auto load_batch = [&](int64_t s0, uint64_t* x) {
+    #pragma unroll
+                    for (int q = 0; q < BW; q += 2) {
+                        const int64_t w = s0 * WORDS + q;
+                        ulonglong2 v = make_ulonglong2(0, 0);
+                        const int64_t at = off + (blocked ? (w >> 2) * (4 * T) + (w & 3) : w);
+                        if (off >= 0 && w + 1 < lim) v = __ldg(reinterpret_cast<const ulonglong2*>(src + at));
+                        else if (off >= 0 && w < lim) v.x = __ldg(src + at);
+                        x[q] = v.x;
+                        x[q + 1] = v.y;
+                    }
+                };
+                if (n_stages > 0) load_batch(0, cur);
+                for (int64_t s0 = 0; s0 < n_stages && !*abort_flag; s0 += PF) {
+                    if (s0 + PF < n_stages) load_batch(s0 + PF, nxt);
+    #pragma unroll
+                    for (int j = 0; j < PF; j++) {
+                        const int64_t s = s0 + j;
+                        if (s >= n_stages) break;
+                        const int64_t G = gstage + s;
+                        const int slot = (int)(G % STAGES);
+                        const uint32_t use = (uint32_t)(G / STAGES);
+                        if (!mbar_wait(&empty_bar[slot], (use & 1u) ^ 1u, abort_flag, WAIT_NS)) break;
+                        if (off >= 0) {
+                            store_row<FMT>(slots + slot * SLOT_BYTES + dst, hrow, cur + j * WORDS);
+                            fence_proxy_async();
+                        }
+                        mbar_arrive(&full_bar[slot]);
+                    }
+    #pragma unroll
+                    for (int q = 0; q < BW; q++) cur[q] = nxt[q];
+                }
             }
             // ---- epilogue: warp w reads lanes 32 (w % 4) .. of accumulator w / 8, columns 128 ((w / 4) % 2) .. ----
             // Warp-uniform, as the tcgen05.ld below needs the whole warp: lane 0 waits for the warp.
@@ -447,13 +515,13 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
                 }
             }
             tc_fence_before();
-        } else if (lane == 0) {
+        } else if (warp == MMA_WARP && lane == 0) {
             // ---- MMA issuer: two M = 128 MMAs per K step, sharing the B tile ----
             tc_fence_after();
             for (int64_t s = 0; s < n_stages; s++) {
                 const int64_t G = gstage + s;
-                const int slot = (int)(G % STAGES);
-                const uint32_t use = (uint32_t)(G / STAGES);
+                const int slot = (int)(G % NST);
+                const uint32_t use = (uint32_t)(G / NST);
                 if (!mbar_wait(&full_bar[slot], use & 1u, abort_flag, first_wait_ns)) break;
                 tc_fence_after();
                 const uint32_t base = smem_u32(slots + slot * SLOT_BYTES);
@@ -471,6 +539,21 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
                 mma_commit(&empty_bar[slot]);
             }
             mma_commit(&acc_bar);
+        } else if (STAGED && warp == LOAD_WARP && lane == 0) {
+            // ---- loader: the raw chunk of block ua (unless diagonal) and of block ub for every stage ----
+            const int64_t cw = cld[wi];
+            const uint64_t* src_a = src + cbase[wi] + ua * T * cw;
+            const uint64_t* src_b = src + cbase[wi] + ub * T * cw;
+            for (int64_t s = 0; s < n_stages; s++) {
+                const int64_t G = gstage + s;
+                const int rs = (int)(G % RAW_STAGES);
+                const uint32_t ruse = (uint32_t)(G / RAW_STAGES);
+                if (!mbar_wait(&raw_empty[rs], (ruse & 1u) ^ 1u, abort_flag, WAIT_NS)) break;
+                mbar_expect_tx(&raw_full[rs], diag ? RAW_BLOCK : 2 * RAW_BLOCK);
+                if (!diag) bulk_copy(raw + rs * RAW_SLOT, src_a + s * 4 * T, RAW_BLOCK, &raw_full[rs]);
+                bulk_copy(raw + rs * RAW_SLOT + RAW_BLOCK, src_b + s * 4 * T, RAW_BLOCK, &raw_full[rs]);
+                raw_issued = G + 1;
+            }
         }
         gstage += n_stages;
         tile_iter += 1;
@@ -478,6 +561,15 @@ __global__ void __launch_bounds__(THREADS, 1) gram_kernel(
         if (*abort_flag) break;
     }
 
+    if (STAGED && warp == LOAD_WARP && lane == 0 && *abort_flag) {
+        // Every bulk copy this CTA issued lands before the CTA exits: wait (bounded) for the last phase issued
+        // on each raw slot (earlier phases of a slot complete first).
+        for (int64_t G = max64(0, raw_issued - RAW_STAGES); G < raw_issued; G++) {
+            const uint64_t t0 = now_ns();
+            while (!mbar_test(&raw_full[G % RAW_STAGES], (uint32_t)(G / RAW_STAGES) & 1u) && now_ns() - t0 < WAIT_NS)
+                __nanosleep(256);
+        }
+    }
     if (warp == MMA_WARP) {
         if (lane == 0 && *abort_flag) {
             // Wait (bounded) for every MMA this CTA issued before its tensor memory is freed.
@@ -560,17 +652,30 @@ std::mutex g_cfg_lock;
 // The MMA thread's wait for a filled stage: WAIT_NS unless a test set it (0 = give up at once).
 uint64_t g_first_wait_ns = WAIT_NS;
 
-template <int FMT>
-int launch_gram(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
-                const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
-                int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t min_count,
-                int32_t* out, uint32_t* surv, int64_t* work_counter, bool blocked, cudaStream_t s) {
+// ETM_GRAM_STAGED=0 in the environment keeps packed e2m1 over blocked rows on the producer-load form
+// (both are exact; the staged form is the faster one on GB300).
+bool staged_enabled() {
+    static const bool on = [] {
+        const char* v = getenv("ETM_GRAM_STAGED");
+        return v == nullptr || v[0] != '0';
+    }();
+    return on;
+}
+
+template <int FMT, bool STAGED>
+int launch_gram_kernel(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
+                       const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
+                       const int64_t* work_off, int64_t n_work, int64_t n_tiles, int64_t chunk_base,
+                       const uint8_t* cls, int32_t min_count, int32_t* out, uint32_t* surv, int64_t* work_counter,
+                       bool blocked, cudaStream_t s) {
+    constexpr int smem = STAGED ? ST_SMEM : SMEM_BYTES;
+    constexpr int threads = STAGED ? ST_THREADS : THREADS;
     static bool configured = false;
     uint64_t first_wait;
     {
         std::lock_guard<std::mutex> guard(g_cfg_lock);
         if (!configured) {
-            ETM_CUDA(cudaFuncSetAttribute(gram_kernel<FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+            ETM_CUDA(cudaFuncSetAttribute(gram_kernel<FMT, STAGED>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
             configured = true;
         }
         first_wait = g_first_wait_ns;
@@ -578,12 +683,27 @@ int launch_gram(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cword
     const int64_t sms = max(1, sm_count());
     const int grid = (int)max64(1, min64(sms, n_tiles > 0 ? n_tiles : sms));
     if (work_counter != nullptr) ETM_CUDA(cudaMemsetAsync(work_counter, 0, sizeof(int64_t), s));
-    gram_kernel<FMT><<<grid, THREADS, SMEM_BYTES, s>>>(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups,
-                                                       work_off, n_work, chunk_base, cls, min_count, out, surv,
-                                                       reinterpret_cast<unsigned long long*>(work_counter),
-                                                       first_wait, blocked);
+    gram_kernel<FMT, STAGED><<<grid, threads, smem, s>>>(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups,
+                                                         work_off, n_work, chunk_base, cls, min_count, out, surv,
+                                                         reinterpret_cast<unsigned long long*>(work_counter),
+                                                         first_wait, blocked);
     ETM_LAUNCHED("gram_tc");
     return ETM_OK;
+}
+
+template <int FMT>
+int launch_gram(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
+                const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
+                int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls, int32_t min_count,
+                int32_t* out, uint32_t* surv, int64_t* work_counter, bool blocked, cudaStream_t s) {
+    if constexpr (FMT == 4) {
+        if (blocked && staged_enabled())
+            return launch_gram_kernel<4, true>(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off,
+                                               n_work, n_tiles, chunk_base, cls, min_count, out, surv, work_counter,
+                                               blocked, s);
+    }
+    return launch_gram_kernel<FMT, false>(cbuf, cbase, cwords, cld, grp_size, cand_off, work_groups, work_off, n_work,
+                                          n_tiles, chunk_base, cls, min_count, out, surv, work_counter, blocked, s);
 }
 
 }  // namespace
