@@ -449,6 +449,117 @@ def deep_sparse_line(pkg, lib, steps: int, warmup: int, with_cpu: bool, cpu_budg
     return line
 
 
+def hbm_kernel_rooflines(pkg, lib, n_rows: int = 20_000_000, reps: int = 3) -> list[dict]:
+    """The AND+popcount and bitvector kernels on the deep sparse workload's shape (20M rows x 2,000 items,
+    planted patterns, generated on the device): per kernel its CUDA-event time (median of ``reps`` after a
+    warm-up), algorithmic bytes, GB/s and fraction of the measured HBM copy peak. Inputs (5 GB of
+    bitvectors) are larger than L2."""
+    import torch
+    from importlib import import_module
+
+    engm = import_module(pkg.__name__ + ".engine")
+    syn = pkg.synthetic
+    peak = _peaks()["hbm_gbs"]
+    st = torch.cuda.current_stream().cuda_stream
+    bv = syn.patterns_bitvecs_device(lib, syn.pattern_spec(), n_rows)
+    n_cols, ld = bv.shape
+    n_words = (n_rows + 63) // 64
+    bvi = bv.view(torch.int64)
+    # The device CSR of the same rows (the bitvector build's input).
+    shifts = torch.arange(64, device="cuda", dtype=torch.int64)
+    keys = []
+    for c0 in range(0, n_cols, 64):
+        bits = ((bvi[c0:c0 + 64][:, :, None] >> shifts) & 1).view(min(64, n_cols - c0), -1)[:, :n_rows]
+        col, row = torch.nonzero(bits, as_tuple=True)
+        keys.append(row * n_cols + (col + c0))
+        del bits
+    k = torch.sort(torch.cat(keys)).values
+    del keys
+    ids = (k % n_cols).to(torch.int32)
+    row_ptr = torch.zeros(n_rows + 1, dtype=torch.int64, device="cuda")
+    row_ptr[1:] = torch.cumsum(torch.bincount(k // n_cols, minlength=n_rows), 0)
+    del k
+    nnz = int(ids.numel())
+    out_bv = torch.empty_like(bvi)
+    counts = torch.empty(n_cols, dtype=torch.int64, device="cuda")
+    eng = engm.Engine()
+    fbv, ldp = eng.gather(bvi.data_ptr(), ld, np.arange(n_cols), n_words)
+    # count_cands: 4,096 random triples of frequent columns as 2-member prefix groups; count_tiles: one group of
+    # 128 columns over every row (the K=2 tile kernel on unprojected words).
+    rng = np.random.default_rng(0)
+    pairs = np.sort(np.stack([rng.choice(n_cols, 3, replace=False) for _ in range(4096)]), axis=1)
+    gen_rows = np.concatenate([pairs[:, [0, 1]], pairs[:, [0, 2]]])
+    gen_rows = np.unique(gen_rows, axis=0).astype(np.int32)
+    gen = engm.Level(torch.from_numpy(gen_rows).cuda(), torch.ones(len(gen_rows), dtype=torch.int32, device="cuda"))
+    G, total, grp_first, grp_size, cand_off = eng.groups(gen)
+    sizes = grp_size[:G].cpu().numpy().astype(np.int64)
+    wg_c, wo_c = eng._work(np.arange(G, dtype=np.int64), sizes * (sizes - 1) // 2)
+    cand_counts = torch.empty(max(1, total), dtype=torch.int32, device="cuda")
+    m_t = 128
+    gen_t = engm.Level(torch.arange(m_t, dtype=torch.int32, device="cuda")[:, None].contiguous(),
+                       torch.ones(m_t, dtype=torch.int32, device="cuda"))
+    Gt, total_t, gf_t, gs_t, co_t = eng.groups(gen_t)
+    nt = (m_t + 63) // 64
+    wg_t, wo_t = eng._work(np.zeros(1, np.int64), np.array([nt * (nt + 1) // 2]))
+    tile_counts = torch.empty(total_t, dtype=torch.int32, device="cuda")
+    n_tp = nt * (nt + 1) // 2
+    n_split = int(max(1, min(-(-n_words // 32), (6 * int(lib.etm_device_sm_count())) // n_tp)))
+    eng_cols = torch.arange(n_cols, dtype=torch.int32, device="cuda")
+    kernels = {
+        "build_bitvecs": (lambda: lib.etm_build_bitvecs(row_ptr.data_ptr(), ids.data_ptr(), nnz, None, 0, n_rows,
+                                                        n_cols, ld, out_bv.data_ptr(), st),
+                          8 * (n_rows + 1) + 4 * nnz + 8 * n_cols * ld, "8(N+1) + 4 nnz read, 8 n_cols W written"),
+        "popcount_cols": (lambda: lib.etm_popcount_cols(bvi.data_ptr(), n_cols, n_words, ld, counts.data_ptr(), st),
+                          8 * n_cols * n_words, "8 n_cols W read"),
+        "gather_cols": (lambda: lib.etm_gather_cols(bvi.data_ptr(), ld, eng_cols.data_ptr(), n_cols, n_words,
+                                                    fbv.data_ptr(), ldp, st),
+                        16 * n_cols * n_words, "8 n_cols W read + written"),
+        "count_cands": (lambda: lib.etm_count_cands(fbv.data_ptr(), ldp, n_words, gen.rows.data_ptr(), 2,
+                                                    grp_first.data_ptr(), grp_size.data_ptr(), cand_off.data_ptr(),
+                                                    wg_c.data_ptr(), wo_c.data_ptr(), G, 0, None,
+                                                    cand_counts.data_ptr(), st),
+                        8 * 3 * n_words * total, "8 k W per candidate (k = 3)"),
+        "count_tiles": (lambda: (tile_counts.zero_(), lib.etm_count_tiles_split(
+                            fbv.data_ptr(), ldp, n_words, gen_t.rows.data_ptr(), 1, gf_t.data_ptr(), gs_t.data_ptr(),
+                            co_t.data_ptr(), wg_t.data_ptr(), wo_t.data_ptr(), 1, n_tp, 0, None, n_split,
+                            tile_counts.data_ptr(), st))[1],
+                        8 * m_t * n_words, "8 m W: each column once (the same-data minimum); word ranges split "
+                                           "across CTAs as the engine splits them"),
+    }
+    out = []
+    for name, (fn, nbytes, how) in kernels.items():
+        times = []
+        for i in range(reps + 1):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            if fn() != 0:
+                raise RuntimeError(f"{name}: {lib.etm_last_error().decode()}")
+            e1.record()
+            torch.cuda.synchronize()
+            if i:
+                times.append(e0.elapsed_time(e1))
+        ms = statistics.median(times)
+        gbs = nbytes / (ms / 1e3) / 1e9
+        out.append({"kernel": name, "ms": round(ms, 3), "algorithmic_bytes": int(nbytes), "bytes": how,
+                    "achieved_gbs": round(gbs, 1), "peak_gbs": peak, "frac": round(gbs / peak, 3)})
+    # The outputs agree with each other: K=1 counts of the rebuilt bitvectors equal those of the originals.
+    assert torch.equal(out_bv, bvi), "build_bitvecs does not reproduce the generator's bitvectors"
+    del bv, bvi, out_bv, fbv, ids, row_ptr
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_hbm_kernels(args) -> None:
+    pkg = _pkg()
+    pkg.build_library()
+    lib = pkg.load_library()
+    rows = hbm_kernel_rooflines(pkg, lib, n_rows=args.hbm_rows)
+    print(json.dumps({"metric": "AND+popcount and bitvector kernels, GB/s against the measured HBM copy peak",
+                      "workload": "hbm_kernels", "config": {"rows": args.hbm_rows, "items": 2_000,
+                                                            "input": "deep sparse planted patterns, device-generated"},
+                      "rooflines": rows}), flush=True)
+
+
 def run_serving(args) -> None:
     """Serving workload: 256 Poisson-arriving requests over 8 resident datasets, p50/p99 latency."""
     import torch
@@ -545,8 +656,10 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="dense_k2", choices=sorted(WORKLOADS) + sorted(TX_WORKLOADS) + ["serving"])
+    ap.add_argument("--workload", default="dense_k2",
+                    choices=sorted(WORKLOADS) + sorted(TX_WORKLOADS) + ["serving", "hbm_kernels"])
     ap.add_argument("--slots", type=int, default=4, help="serving: requests on the GPU at once")
+    ap.add_argument("--hbm-rows", type=int, default=20_000_000, help="hbm_kernels: transactions of the input")
     ap.add_argument("--serving-scale", type=float, default=1.0, help="serving: dataset row scale")
     ap.add_argument("--serving-requests", type=int, default=256)
     ap.add_argument("--method", default=None, choices=["popcount", "tensor"])
@@ -564,6 +677,13 @@ def main() -> None:
     ap.add_argument("--no-pipeline", action="store_true",
                     help="project and count chunks in turn on one stream (per-kernel times without overlap)")
     args = ap.parse_args()
+    if args.workload == "hbm_kernels":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the kernel roofline workload has no CPU arm"}))
+            return
+        if int(os.environ.get("RANK", "0")) == 0:
+            run_hbm_kernels(args)
+        return
     if args.workload == "serving":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the serving workload has no CPU arm"}))

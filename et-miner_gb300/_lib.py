@@ -115,6 +115,8 @@ SIGNATURES: dict[str, tuple] = {
     "etm_device_status": (ctypes.c_int, [_P]),
     "etm_level_compact": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _P, _P, _P, _I64, _I64, _I32, _P, _P, _I64, _P, _P, _I64, _P]),
     "etm_level_compact_static": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _P, _P, _P, _I64, _I64, _I32, _P, _P, _I64, _P, _P]),
+    "etm_count_tiles_split": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64, _I64, _I64, _P, _I32,
+                                             _P, _P]),
     "etm_count_tiles_sel": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P,
                                            _P]),
     "etm_count_cands_sel": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P,

@@ -43,6 +43,43 @@ __global__ void __launch_bounds__(BUILD_THREADS) build_bitvecs_kernel(
     }
 }
 
+// Shared-memory form for up to SMEM_BUILD_COLS columns: the block's 256 rows are 4 words of every column,
+// held in shared memory (n_cols x 32 bytes); entries OR their bits there, then the block writes each of its
+// words once, 32 contiguous bytes per column. Every output word is written by exactly one block, so the
+// output needs no zeroing first and no global atomics run.
+constexpr int SMEM_BUILD_COLS = 3072;  // 96 KB of shared memory
+__global__ void __launch_bounds__(BUILD_THREADS) build_bitvecs_smem_kernel(
+    const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ ids, int64_t nnz, const int32_t* __restrict__ lut,
+    int64_t lut_size, int64_t n_rows, int64_t n_cols, int64_t ld, uint64_t* __restrict__ out) {
+    extern __shared__ unsigned long long words[];  // [n_cols][4]
+    __shared__ int64_t ptr[BUILD_ROWS + 1];
+    const int64_t r0 = (int64_t)blockIdx.x * BUILD_ROWS;
+    const int nr = (int)min64(BUILD_ROWS, n_rows - r0);
+    for (int t = threadIdx.x; t <= nr; t += blockDim.x) ptr[t] = row_ptr[r0 + t];
+    for (int64_t t = threadIdx.x; t < n_cols * 4; t += blockDim.x) words[t] = 0ULL;
+    __syncthreads();
+    const int64_t e0 = max64(ptr[0], 0), e1 = min64(ptr[nr], nnz);
+    for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        int lo = 0, hi = nr;
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (ptr[mid] <= e) lo = mid;
+            else hi = mid;
+        }
+        if (e < ptr[lo] || e >= ptr[lo + 1]) continue;
+        int64_t col = ids[e];
+        if (lut) col = (col >= 0 && col < lut_size) ? (int64_t)lut[col] : -1;
+        if (col < 0 || col >= n_cols) continue;
+        atomicOr(words + col * 4 + (lo >> 6), 1ULL << (lo & 63));
+    }
+    __syncthreads();
+    const int64_t w0 = r0 >> 6;
+    for (int64_t t = threadIdx.x; t < n_cols * 4; t += blockDim.x) {
+        const int64_t w = w0 + (t & 3);
+        if (w < ld) out[(t >> 2) * ld + w] = words[t];
+    }
+}
+
 constexpr int POP_THREADS = 256;
 constexpr int64_t POP_SEG_WORDS = 1 << 16;  // words per block: a column is split over several blocks
 
@@ -199,9 +236,25 @@ extern "C" int etm_build_bitvecs(const int64_t* row_ptr, const int32_t* ids, int
     ETM_REQUIRE(n_rows < (1LL << 31), ETM_EINVAL, "etm_build_bitvecs: n_rows must be < 2^31");
     cudaStream_t s = as_stream(stream);
     if (n_cols == 0 || ld == 0) return ETM_OK;
+    const int64_t blocks = ceil_div<int64_t>(n_rows, BUILD_ROWS);
+    if (n_cols <= SMEM_BUILD_COLS && n_rows > 0) {
+        // The blocks write words [0, 4 blocks) of every column; words past that (a wider ld) are zeroed.
+        if (ld > 4 * blocks)
+            ETM_CUDA(cudaMemset2DAsync(out_bv + 4 * blocks, ld * 8, 0, (size_t)(ld - 4 * blocks) * 8, (size_t)n_cols, s));
+        const size_t smem = (size_t)n_cols * 32;
+        static bool configured = false;
+        if (!configured) {
+            ETM_CUDA(cudaFuncSetAttribute(build_bitvecs_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          SMEM_BUILD_COLS * 32));
+            configured = true;
+        }
+        build_bitvecs_smem_kernel<<<(unsigned)blocks, BUILD_THREADS, smem, s>>>(row_ptr, ids, nnz, lut, lut_size, n_rows,
+                                                                               n_cols, ld, out_bv);
+        ETM_LAUNCHED("build_bitvecs");
+        return ETM_OK;
+    }
     ETM_CUDA(cudaMemsetAsync(out_bv, 0, (size_t)n_cols * ld * 8, s));
     if (n_rows == 0) return ETM_OK;
-    const int64_t blocks = ceil_div<int64_t>(n_rows, BUILD_ROWS);
     build_bitvecs_kernel<<<(unsigned)blocks, BUILD_THREADS, 0, s>>>(row_ptr, ids, nnz, lut, lut_size, n_rows, n_cols, ld,
                                                                     reinterpret_cast<unsigned long long*>(out_bv));
     ETM_LAUNCHED("build_bitvecs");

@@ -54,14 +54,19 @@ __global__ void __launch_bounds__(TILE_THREADS) count_tiles_popc_kernel(
     const int64_t* __restrict__ cwords, const int64_t* __restrict__ cld, const int32_t* __restrict__ rows, int width,
     const int64_t* __restrict__ grp_first, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
     const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
-    const uint8_t* __restrict__ cls, int32_t* __restrict__ out, int32_t min_count, uint32_t* __restrict__ surv) {
+    const uint8_t* __restrict__ cls, int32_t* __restrict__ out, int32_t min_count, uint32_t* __restrict__ surv,
+    int n_split) {
     __shared__ TileShared sh;
     const int tid = threadIdx.x;
     const int ty = tid >> 4, tx = tid & 15;
-    const int64_t total = work_off[n_work];
+    // With n_split > 1 every tile-pair's word range is cut into n_split parts counted by different CTAs, which
+    // add their partial counts into `out` (zeroed by the caller): few tile-pairs over many rows still fill the GPU.
+    const int64_t total = work_off[n_work] * n_split;
     const int plen = PROJ ? 0 : width - 1;
 
-    for (int64_t tp = blockIdx.x; tp < total; tp += gridDim.x) {
+    for (int64_t unit = blockIdx.x; unit < total; unit += gridDim.x) {
+        const int64_t tp = unit / n_split;
+        const int part = (int)(unit - tp * n_split);
         const int64_t wi = upper_find(work_off, n_work, tp);
         const int64_t g = work_groups[wi];
         const int64_t m = grp_size[g];
@@ -72,7 +77,10 @@ __global__ void __launch_bounds__(TILE_THREADS) count_tiles_popc_kernel(
         const int64_t first = PROJ ? 0 : grp_first[g];  // the projected source needs no rows
         const int64_t cb = cand_off[g] - chunk_base;
         const int64_t words = PROJ ? cwords[wi] : n_words;
-        const int64_t n_slabs = ceil_div<int64_t>(words, WCH);
+        const int64_t n_slabs_all = ceil_div<int64_t>(words, WCH);
+        const int64_t per = ceil_div<int64_t>(n_slabs_all, n_split);
+        const int64_t s_first = part * per;
+        const int64_t n_slabs = min64(n_slabs_all, s_first + per);
 
         if (tid < TT) {
             const int64_t ia = ti * TT + tid, ib = tj * TT + tid;
@@ -109,7 +117,7 @@ __global__ void __launch_bounds__(TILE_THREADS) count_tiles_popc_kernel(
 #pragma unroll
             for (int c = 0; c < 4; c++) acc[r][c] = 0;
 
-        for (int64_t s = 0; s < n_slabs; s++) {
+        for (int64_t s = s_first; s < n_slabs; s++) {
             const int64_t w0 = s * WCH;
             if (!PROJ) {
                 if (tid < WCH) {
@@ -162,7 +170,13 @@ __global__ void __launch_bounds__(TILE_THREADS) count_tiles_popc_kernel(
                 const int64_t j = tj * TT + tx + 16 * c;
                 if (i < j && j < m) {
                     const int64_t t = cb + tri_index(i, j, m);
-                    if (cls == nullptr || cls[t] == ETM_CAND_COUNT) emit_count(out, surv, t, (int32_t)acc[r][c], min_count);
+                    if (cls == nullptr || cls[t] == ETM_CAND_COUNT) {
+                        if (n_split > 1) {
+                            if (acc[r][c]) atomicAdd(out + t, (int32_t)acc[r][c]);
+                        } else {
+                            emit_count(out, surv, t, (int32_t)acc[r][c], min_count);
+                        }
+                    }
                 }
             }
         }
@@ -231,7 +245,7 @@ int count_tiles_popcount(const uint64_t* fbv, int64_t ld, int64_t n_words, const
     count_tiles_popc_kernel<false><<<grid, TILE_THREADS, 0, s>>>(fbv, ld, n_words, nullptr, nullptr, nullptr, rows,
                                                                  width, grp_first, grp_size, cand_off, work_groups,
                                                                  work_off, n_work, chunk_base, cls, out, min_count,
-                                                                 surv);
+                                                                 surv, 1);
     ETM_LAUNCHED("count_tiles_popc");
     return ETM_OK;
 }
@@ -243,7 +257,7 @@ int count_tiles_proj_popcount(const uint64_t* cbuf, const int64_t* cbase, const 
     const int grid = max(1, sm_count()) * 6;
     count_tiles_popc_kernel<true><<<grid, TILE_THREADS, 0, s>>>(cbuf, 0, 0, cbase, cwords, cld, nullptr, 1, nullptr,
                                                                 grp_size, cand_off, work_groups, work_off, n_work,
-                                                                chunk_base, cls, out, min_count, surv);
+                                                                chunk_base, cls, out, min_count, surv, 1);
     ETM_LAUNCHED("count_tiles_proj_popc");
     return ETM_OK;
 }
@@ -266,6 +280,28 @@ extern "C" int etm_count_tiles(const uint64_t* fbv, int64_t ld, int64_t n_words,
     ETM_REQUIRE(method == ETM_METHOD_POPCOUNT, ETM_EINVAL, "etm_count_tiles: unknown method %d", method);
     return etm::count_tiles_popcount(fbv, ld, n_words, rows, width, grp_first, grp_size, cand_off, work_groups,
                                      work_off, n_work, chunk_base, cls, out_counts, -1, s, 0, nullptr);
+}
+
+extern "C" int etm_count_tiles_split(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows,
+                                     int32_t width, const int64_t* grp_first, const int32_t* grp_size,
+                                     const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
+                                     int64_t n_work, int64_t n_tiles, int64_t chunk_base, const uint8_t* cls,
+                                     int32_t n_split, int32_t* out_counts, void* stream) {
+    ETM_REQUIRE(width >= 1 && width <= MAXP, ETM_EINVAL, "etm_count_tiles_split: width %d out of range", width);
+    ETM_REQUIRE(ld % WCH == 0 && ld >= n_words, ETM_EINVAL,
+                "etm_count_tiles_split: ld must be a multiple of %d >= n_words", WCH);
+    ETM_REQUIRE((reinterpret_cast<uintptr_t>(fbv) & 15) == 0, ETM_EINVAL,
+                "etm_count_tiles_split: fbv must be 16-byte aligned");
+    ETM_REQUIRE(n_split >= 1 && n_split <= 65536, ETM_EINVAL, "etm_count_tiles_split: n_split %d out of range", n_split);
+    if (n_work <= 0) return ETM_OK;
+    const int64_t cap = (int64_t)max(1, sm_count()) * 6;
+    const int64_t units = (n_tiles > 0 ? n_tiles : cap) * n_split;
+    const int grid = (int)max64(1, min64(cap, units));
+    count_tiles_popc_kernel<false><<<grid, TILE_THREADS, 0, as_stream(stream)>>>(
+        fbv, ld, n_words, nullptr, nullptr, nullptr, rows, width, grp_first, grp_size, cand_off, work_groups, work_off,
+        n_work, chunk_base, cls, out_counts, 0, nullptr, n_split);
+    ETM_LAUNCHED("count_tiles_popc");
+    return ETM_OK;
 }
 
 extern "C" int etm_count_tiles_sel(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows,

@@ -342,6 +342,11 @@ class Engine:
         self._waits_pending = False
         self._side: torch.cuda.Stream | None = None
 
+    def _sms(self) -> int:
+        if getattr(self, "_sm_count", None) is None:
+            self._sm_count = max(1, int(self.lib.etm_device_sm_count()))
+        return self._sm_count
+
     def _side_stream(self) -> torch.cuda.Stream:
         """The stream projection runs on beside the counting kernels (created on first use)."""
         if self._side is None:
@@ -477,8 +482,15 @@ class Engine:
                     macs=float((m * (m - 1) / 2 * cnt.astype(np.float64)).sum()))
 
     def _count_prepped(self, prep, grp_size, cand_off, base, cls, counts, method, sel=None):
-        """The tile-pair counts of a prepared projection (one launch on the current stream)."""
-        prep["d"].record_stream(torch.cuda.current_stream())
+        """The tile-pair counts of a prepared projection (one launch on the current stream).
+
+        Every tensor the projection made on the side stream and the counting reads here is recorded on this
+        stream, so the caching allocator does not hand its memory to a later side-stream allocation (a grown
+        scratch buffer) while this stream may still read it.
+        """
+        cur = torch.cuda.current_stream()
+        prep["d"].record_stream(cur)
+        prep["cbuf"].record_stream(cur)
         self._count_words(prep["cbuf"], prep["cbase"], prep["cwords"], prep["cld"], grp_size, cand_off, prep["wg"],
                           prep["wo"], prep["n"], prep["n_tiles"], base, cls, counts, method, prep["nbytes"],
                           prep["macs"], sel, prep["blocked"])
@@ -688,6 +700,21 @@ class Engine:
                 bits = self.scratch.get("chunk_bits", (n_c + 31) // 32 + 1, torch.int32)
                 bits.zero_()
             sel = (mc, bits) if (self.fused and not row_wise) else None
+            m = sizes[g0:g1]
+            ids = np.arange(g0, g1, dtype=np.int64)
+            small = m <= self.small_group
+            pr = proj[g0:g1]
+            # Tile groups too few to fill the GPU (few members over many rows) split their word ranges across
+            # CTAs, which add partial counts: the chunk's counts start at zero and its bits come from a
+            # threshold pass at the end (the fused kernels leave non-survivors at zero, so the pass agrees).
+            tile_ids = ids[~small & ~pr] if not row_wise else ids[:0]
+            n_split = 1
+            if len(tile_ids):
+                nt_t = (sizes[tile_ids] + TILE - 1) // TILE
+                n_tp = int((nt_t * (nt_t + 1) // 2).sum())
+                n_split = int(max(1, min(-(-n_words // 32), (6 * self._sms()) // max(1, n_tp))))
+            if n_split > 1:
+                counts.zero_()
             if classify:
                 if sel is None:
                     fn = lambda: self.lib.etm_classify(  # noqa: E731
@@ -699,10 +726,6 @@ class Engine:
                         _p(cand_off), g0, g1, mode, mc, _p(cls), _p(counts), _p(bits), _stream())
                 check(self._launch("classify", n_c * 5, fn), "etm_classify")
                 self.launches += 1
-            m = sizes[g0:g1]
-            ids = np.arange(g0, g1, dtype=np.int64)
-            small = m <= self.small_group
-            pr = proj[g0:g1]
             if k2_rows:
                 stats.row_wise = True
                 # K=2 from the transactions (one group of every generator): pair counts by row-wise increments.
@@ -778,7 +801,11 @@ class Engine:
                         # this kind under the tensor method hold more than 2^24 rows (past the f32-exact range
                         # of the Gram), so these tiles always count on the CUDA cores.
                         nbytes = int((mg + width - 1).sum()) * n_words * 8
-                        if sel is None:
+                        if n_split > 1:
+                            fn = lambda: self.lib.etm_count_tiles_split(  # noqa: E731
+                                _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
+                                _p(wg), _p(wo), len(bg), int(bw.sum()), base, _p(cls), n_split, _p(counts), _stream())
+                        elif sel is None:
                             fn = lambda: self.lib.etm_count_tiles(  # noqa: E731
                                 _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
                                 _p(wg), _p(wo), len(bg), base, _p(cls), 0, _p(counts), _stream())
@@ -791,7 +818,7 @@ class Engine:
                     self.launches += 1
             if pipelined and c + 1 < len(chunks):
                 prep(c + 1)  # overlaps this chunk's counting and the host wait in its compaction
-            if self.fused and row_wise:
+            if self.fused and (row_wise or n_split > 1):
                 check(self._launch("threshold_bits", n_c * (5 if classify else 4), lambda: self.lib.etm_threshold_bits(
                     _p(counts), _p(cls), n_c, mc, _p(bits), _stream())), "etm_threshold_bits")
                 self.launches += 1

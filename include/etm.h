@@ -337,6 +337,19 @@ int etm_device_status(void* stream);
 int etm_set_wait_limits(int64_t gram_first_wait_ns, int64_t proj_first_wait_ns);
 
 /*
+ * etm_count_tiles (popcount method) with each tile-pair's word range cut into
+ * n_split parts counted by different CTAs, which atomically add their partial
+ * counts into out_counts: the caller zeroes the counted candidates' slots
+ * first. For groups with few members over many rows (K=2 past the Gram's 2^24
+ * rows), where the tile-pairs alone cannot fill the GPU. n_tiles =
+ * work_off[n_work] sizes the grid. Dense counts (no threshold).
+ */
+int etm_count_tiles_split(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
+                          const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
+                          const int64_t* work_groups, const int64_t* work_off, int64_t n_work, int64_t n_tiles,
+                          int64_t chunk_base, const uint8_t* cls, int32_t n_split, int32_t* out_counts, void* stream);
+
+/*
  * The fused-threshold ("select") forms of the counting entry points, after
  * count_shared_tiled_fused (gpu/kernels/_src/shared_tiled.cu:246-280): each
  * takes min_count and a survivor bitmask surv_bits (uint32 words; bit t % 32

@@ -496,3 +496,43 @@ def test_triple_counts_rows_match_host(pkg, lib, long_rows):
                                     d[7].data_ptr(), base, n_c, d[8].data_ptr(), out.data_ptr(), _stream())
     assert st == 0, lib.etm_last_error()
     assert np.array_equal(out.cpu().numpy(), expect)
+
+
+@pytest.mark.parametrize("n_split", [1, 7, 94])
+def test_split_tiles_add_up_to_the_whole_counts(pkg, lib, n_split):
+    """etm_count_tiles_split: the word range of every tile-pair cut into n_split parts whose partial counts
+    are added atomically gives the counts of etm_count_tiles, including word tails and a prefix AND."""
+    import torch
+
+    from importlib import import_module
+
+    engm = import_module(pkg.__name__ + ".engine")
+    eng = engm.Engine(method="popcount")
+    rng = np.random.default_rng(n_split)
+    n_f, n_words = 150, 2999
+    bv = rng.integers(0, 2**63, size=(n_f, n_words), dtype=np.int64)
+    bv &= rng.integers(0, 2**63, size=(n_f, n_words), dtype=np.int64)
+    dev = torch.from_numpy(bv).cuda()
+    fbv, ldp = eng.gather(dev.data_ptr(), n_words, np.arange(n_f), n_words)
+    # Width 2: prefix column 0 with members 1..149 (one group, the prefix ANDed in per word).
+    rows = np.stack([np.zeros(n_f - 1, np.int32), np.arange(1, n_f, dtype=np.int32)], axis=1)
+    gen = engm.Level(torch.from_numpy(rows).cuda(), torch.ones(n_f - 1, dtype=torch.int32, device="cuda"))
+    G, total, gf, gs, co = eng.groups(gen)
+    m = n_f - 1
+    nt = (m + 63) // 64
+    wg, wo = eng._work(np.zeros(1, np.int64), np.array([nt * (nt + 1) // 2]))
+    st = torch.cuda.current_stream().cuda_stream
+    want = torch.full((total,), -5, dtype=torch.int32, device="cuda")
+    assert lib.etm_count_tiles(fbv.data_ptr(), ldp, n_words, gen.rows.data_ptr(), 2, gf.data_ptr(), gs.data_ptr(),
+                               co.data_ptr(), wg.data_ptr(), wo.data_ptr(), 1, 0, None, 0, want.data_ptr(), st) == 0
+    got = torch.zeros(total, dtype=torch.int32, device="cuda")
+    assert lib.etm_count_tiles_split(fbv.data_ptr(), ldp, n_words, gen.rows.data_ptr(), 2, gf.data_ptr(),
+                                     gs.data_ptr(), co.data_ptr(), wg.data_ptr(), wo.data_ptr(), 1,
+                                     nt * (nt + 1) // 2, 0, None, n_split, got.data_ptr(), st) == 0, \
+        lib.etm_last_error()
+    w = want.cpu().numpy()
+    assert (w >= 0).all()
+    assert np.array_equal(got.cpu().numpy(), w)
+    ii, jj = np.triu_indices(m, 1)
+    host = np.bitwise_count(bv.view(np.uint64)[0] & bv.view(np.uint64)[1 + ii] & bv.view(np.uint64)[1 + jj]).sum(1)
+    assert np.array_equal(w, host)
