@@ -750,7 +750,8 @@ def main() -> None:
     start.record()
     for _ in range(args.steps):
         out = one(eng)
-        assert [s.n_frequent for s in out.stats] == ref_sizes
+        sizes_now = [s.n_frequent for s in out.stats]
+        assert sizes_now == ref_sizes, f"level sizes changed between mines: {sizes_now} vs {ref_sizes}"
     end.record()
     torch.cuda.synchronize()
     barrier()

@@ -452,10 +452,10 @@ __global__ void __launch_bounds__(STAGED ? ST_THREADS : THREADS, 1) gram_kernel(
                 }
             }
             // ---- epilogue: warp w reads lanes 32 (w % 4) .. of accumulator w / 8, columns 128 ((w / 4) % 2) .. ----
-            // Warp-uniform, as the tcgen05.ld below needs the whole warp: lane 0 waits for the warp.
-            int acc_ready = 1;
-            if (lane == 0 && n_stages > 0) acc_ready = mbar_wait(&acc_bar, tile_iter & 1u, abort_flag, WAIT_NS);
-            const bool ok = __shfl_sync(0xffffffffu, acc_ready, 0) != 0;
+            // Every lane observes the accumulator barrier itself (its own acquire before its tcgen05 fence), and
+            // the warp takes one decision, as the tcgen05.ld below needs the whole warp.
+            const bool got_acc = n_stages == 0 || mbar_wait(&acc_bar, tile_iter & 1u, abort_flag, WAIT_NS);
+            const bool ok = __all_sync(0xffffffffu, got_acc);
             if (ok) {
                 tc_fence_after();
                 const int lane_base = (warp & 3) * 32;
