@@ -122,7 +122,8 @@ SIGNATURES: dict[str, tuple] = {
     "etm_count_cands_sel": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P,
                                            _P]),
     "etm_count_tiles_proj_sel": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P, _P]),
-    "etm_classify_sel": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _P, _P, _I64, _I64, _I32, _I32, _P, _P, _P, _P]),
+    "etm_classify_sel": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _P, _P, _I64, _I64, _I32, _I32, _P, _I64, _P, _P,
+                                        _I64, _P, _I64, _P, _P, _P, _P]),
     "etm_threshold_bits": (ctypes.c_int, [_P, _P, _I64, _I32, _P, _P]),
     "etm_level_compact_bits": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _P, _P, _P, _I64, _I64, _P, _P, _I64, _P, _P, _I64,
                                               _P]),

@@ -40,6 +40,90 @@ __device__ int64_t find_subset(const int32_t* __restrict__ rows, int64_t n, int 
     return -1;
 }
 
+// Row of the sorted level rows[n][m] equal to items[0..m), or -1.
+__device__ int64_t find_items(const int32_t* __restrict__ rows, int64_t n, int m, const int32_t* items) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        const int64_t mid = lo + ((hi - lo) >> 1);
+        const int32_t* r = rows + mid * m;
+        int cmp = 0;
+        for (int t = 0; t < m && cmp == 0; t++) {
+            const int32_t x = __ldg(r + t);
+            cmp = x < items[t] ? -1 : (x > items[t] ? 1 : 0);
+        }
+        if (cmp == 0) return mid;
+        if (cmp < 0) lo = mid + 1;
+        else hi = mid;
+    }
+    return -1;
+}
+
+// ---- deduction bounds ----------------------------------------------------------
+//
+// The count of an itemset X of k items is bounded by inclusion-exclusion over its subsets (Calders &
+// Goethals 2002; the depth <= 3 rules of _deduce, gpu/kernels/_src/_subset_index.cu:95-136):
+//   upper u = min( min_a s(X-a), min_{a<b<c} s(X-a)+s(X-b)+s(X-c) - s(X-ab)-s(X-ac)-s(X-bc) + s(X-abc) )
+//   lower l = max( 0, max_{a<b} s(X-a) + s(X-b) - s(X-ab) )
+// with s(X-a) from level k-1, s(X-ab) from level k-2 and s(X-abc) from level k-3 (the empty set's count,
+// the row count, at k = 3). u < min_count: X is infrequent; l = u: X's count is u. Both hold exactly for
+// integer counts, so settling a candidate by them changes no result.
+constexpr int BOUNDS_MAX_K = 24;
+
+struct DeepLevels {
+    const int32_t* rows2;   // level k-2: rows [n2][k-2], sorted, and counts
+    int64_t n2;
+    const int32_t* counts2;
+    const int32_t* rows3;   // level k-3 (k > 3)
+    int64_t n3;
+    const int32_t* counts3;
+    int64_t n_total;        // the row count: s of the empty set (k = 3)
+};
+
+// ETM_CAND_SKIP, ETM_CAND_INFER (count in *inferred) or ETM_CAND_COUNT for X = items[0..k), c1[t] = s(X - item t).
+__device__ __noinline__ uint8_t deduce(const int32_t* items, int k, const int32_t* c1, const DeepLevels& deep,
+                                       int32_t min_count, int32_t* inferred) {
+    int32_t s2[BOUNDS_MAX_K * (BOUNDS_MAX_K - 1) / 2];
+    int32_t sub[BOUNDS_MAX_K];
+    int64_t lower = 0, upper = 0x7FFFFFFF;
+    for (int t = 0; t < k; t++) upper = min(upper, (int64_t)c1[t]);
+    for (int j = 1; j < k; j++) {
+        for (int i = 0; i < j; i++) {
+            int n = 0;
+            for (int t = 0; t < k; t++)
+                if (t != i && t != j) sub[n++] = items[t];
+            const int64_t r = find_items(deep.rows2, deep.n2, k - 2, sub);
+            if (r < 0) return ETM_CAND_COUNT;  // an infrequent (k-2)-subset: counting settles it
+            const int32_t c = deep.counts2[r];
+            s2[j * (j - 1) / 2 + i] = c;
+            lower = max(lower, (int64_t)c1[i] + c1[j] - c);
+        }
+    }
+    for (int l = 2; l < k && lower < upper && upper >= min_count; l++) {
+        for (int j = 1; j < l && lower < upper; j++) {
+            for (int i = 0; i < j && lower < upper; i++) {
+                int64_t c3 = deep.n_total;
+                if (k > 3) {
+                    int n = 0;
+                    for (int t = 0; t < k; t++)
+                        if (t != i && t != j && t != l) sub[n++] = items[t];
+                    const int64_t r = find_items(deep.rows3, deep.n3, k - 3, sub);
+                    if (r < 0) return ETM_CAND_COUNT;
+                    c3 = deep.counts3[r];
+                }
+                const int64_t u3 = (int64_t)c1[i] + c1[j] + c1[l] - s2[j * (j - 1) / 2 + i] - s2[l * (l - 1) / 2 + i] -
+                                   s2[l * (l - 1) / 2 + j] + c3;
+                upper = min(upper, u3);
+            }
+        }
+    }
+    if (upper < min_count) return ETM_CAND_SKIP;
+    if (lower == upper) {
+        *inferred = (int32_t)upper;
+        return ETM_CAND_INFER;
+    }
+    return ETM_CAND_COUNT;
+}
+
 // ---- prefix groups --------------------------------------------------------
 
 struct RunStart {
@@ -132,11 +216,13 @@ __global__ void classify_kernel(const int32_t* __restrict__ rows, int width, int
                                 const int64_t* __restrict__ grp_first, const int32_t* __restrict__ grp_size,
                                 const int64_t* __restrict__ cand_off, int64_t g0, int64_t g1, int mode,
                                 uint8_t* __restrict__ out_cls, int32_t* __restrict__ out_counts, int32_t min_count,
-                                uint32_t* __restrict__ surv) {
+                                uint32_t* __restrict__ surv, DeepLevels deep) {
     const int64_t base = cand_off[g0];
     const int64_t n = cand_off[g1] - base;
     const bool prune = mode & ETM_SUBSET_PRUNE, infer = (mode & ETM_SUBSET_INFER) && free_flags && counts;
+    const bool bounds = infer && (mode & ETM_SUBSET_BOUNDS) && width + 1 <= BOUNDS_MAX_K && deep.rows2 != nullptr;
     int32_t items[MAXK];
+    int32_t c1[BOUNDS_MAX_K];
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
         const Cand c = decode_candidate(cand_off, grp_size, g0, g1, base + t);
         const int64_t first = grp_first[c.g];
@@ -152,6 +238,7 @@ __global__ void classify_kernel(const int32_t* __restrict__ rows, int width, int
             } else if (infer) {
                 lowest = min(lowest, counts[r]);
                 not_free |= free_flags[r] == 0;
+                if (bounds) c1[d] = counts[r];
             }
         }
         if (missing) {
@@ -160,10 +247,18 @@ __global__ void classify_kernel(const int32_t* __restrict__ rows, int width, int
             const int64_t ri = first + c.i, rj = first + c.j;
             lowest = min(lowest, min(counts[ri], counts[rj]));
             not_free |= (free_flags[ri] == 0) | (free_flags[rj] == 0);
+            int32_t value = lowest;
             if (not_free) {
                 cls = ETM_CAND_INFER;
-                out_counts[t] = lowest;
-                if (surv != nullptr && lowest >= min_count) atomicOr(surv + (t >> 5), 1u << (t & 31));
+            } else if (bounds) {
+                // X without s_i is member j's row, X without s_j is member i's row.
+                c1[width - 1] = counts[rj];
+                c1[width] = counts[ri];
+                cls = deduce(items, width + 1, c1, deep, min_count, &value);
+            }
+            if (cls == ETM_CAND_INFER) {
+                out_counts[t] = value;
+                if (surv != nullptr && value >= min_count) atomicOr(surv + (t >> 5), 1u << (t & 31));
             }
         }
         out_cls[t] = cls;
@@ -345,8 +440,8 @@ extern "C" int etm_classify(const int32_t* rows, int32_t width, int64_t n_rows, 
     ETM_REQUIRE(g0 >= 0 && g1 >= g0, ETM_EINVAL, "etm_classify: bad group range");
     if (g1 == g0) return ETM_OK;
     classify_kernel<<<max(1, sm_count()) * 8, 256, 0, as_stream(stream)>>>(
-        rows, width, n_rows, counts, free_flags, grp_first, grp_size, cand_off, g0, g1, mode, out_cls, out_counts, 0,
-        nullptr);
+        rows, width, n_rows, counts, free_flags, grp_first, grp_size, cand_off, g0, g1, mode & ~ETM_SUBSET_BOUNDS,
+        out_cls, out_counts, 0, nullptr, DeepLevels{nullptr, 0, nullptr, nullptr, 0, nullptr, 0});
     ETM_LAUNCHED("classify");
     return ETM_OK;
 }
@@ -354,14 +449,21 @@ extern "C" int etm_classify(const int32_t* rows, int32_t width, int64_t n_rows, 
 extern "C" int etm_classify_sel(const int32_t* rows, int32_t width, int64_t n_rows, const int32_t* counts,
                                 const uint8_t* free_flags, const int64_t* grp_first, const int32_t* grp_size,
                                 const int64_t* cand_off, int64_t g0, int64_t g1, int32_t mode, int32_t min_count,
-                                uint8_t* out_cls, int32_t* out_counts, uint32_t* surv_bits, void* stream) {
+                                const int32_t* deep2_rows, int64_t deep2_n, const int32_t* deep2_counts,
+                                const int32_t* deep3_rows, int64_t deep3_n, const int32_t* deep3_counts,
+                                int64_t n_transactions, uint8_t* out_cls, int32_t* out_counts, uint32_t* surv_bits,
+                                void* stream) {
     ETM_REQUIRE(width >= 1 && width < MAXK, ETM_EINVAL, "etm_classify_sel: width %d out of range", width);
     ETM_REQUIRE(g0 >= 0 && g1 >= g0, ETM_EINVAL, "etm_classify_sel: bad group range");
     ETM_REQUIRE(surv_bits != nullptr, ETM_EINVAL, "etm_classify_sel: surv_bits is required");
+    ETM_REQUIRE(!(mode & ETM_SUBSET_BOUNDS) || (deep2_rows != nullptr && (width + 1 <= 3 || deep3_rows != nullptr)),
+                ETM_EINVAL, "etm_classify_sel: the deduction bounds need levels k-2 and (k > 3) k-3");
     if (g1 == g0) return ETM_OK;
+    const DeepLevels deep{(mode & ETM_SUBSET_BOUNDS) ? deep2_rows : nullptr, deep2_n, deep2_counts, deep3_rows, deep3_n,
+                          deep3_counts, n_transactions};
     classify_kernel<<<max(1, sm_count()) * 8, 256, 0, as_stream(stream)>>>(
         rows, width, n_rows, counts, free_flags, grp_first, grp_size, cand_off, g0, g1, mode, out_cls, out_counts,
-        min_count, surv_bits);
+        min_count, surv_bits, deep);
     ETM_LAUNCHED("classify");
     return ETM_OK;
 }

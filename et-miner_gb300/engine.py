@@ -140,6 +140,8 @@ class LevelStats:
     n_chunks: int = 0
     launches: int = 0
     row_wise: bool = False  # counted from the transactions (row-wise K=2 / K=3 kernels)
+    n_inferred: int = 0  # candidates whose count the subset test or the deduction bounds settled (class_stats)
+    n_skipped: int = 0  # candidates the subset test or the bounds showed infrequent (class_stats)
 
 
 @dataclass
@@ -298,7 +300,7 @@ class Engine:
                  form: str = "batched", chunk_cands: int = CHUNK_CANDS, small_group: int = SMALL_GROUP,
                  project: bool = True, proj_density: float = PROJ_DENSITY, proj_bytes: int = PROJ_BYTES,
                  tc_elem: int = DEFAULT_TC_ELEM, pipeline: bool = True, autotune: "Autotuner | bool | None" = None,
-                 fused: bool = True):
+                 fused: bool = True, deduction_bounds: bool = True):
         if not torch.cuda.is_available():
             raise RuntimeError("the GB300 engine needs a CUDA device; there is no CPU fallback")
         self.lib = load_library()
@@ -324,6 +326,13 @@ class Engine:
         #: Fused threshold: the counting kernels write only the counts reaching min_count and a survivor bit each;
         #: compaction scans the bitmask (a 32nd of the dense counts). False: dense counts, dense compaction.
         self.fused = bool(fused)
+        #: Under count inference, settle candidates by the deduction bounds of depth <= 3 from levels k-2 and
+        #: k-3 (on by default in the reference's GPU route, gpu/row_split.py:541-546, 629); needs fused.
+        self.deduction_bounds = bool(deduction_bounds)
+        #: (level k-2, level k-3 or None, N) of the level being counted, for the deduction bounds.
+        self._deep = None
+        #: When set, each level's stats count the candidates classified INFER and SKIP (one extra pass per chunk).
+        self.class_stats = False
         #: K=2 counts row-wise from the transactions (when given) while
         #: sum C(len,2) / (pairs x words) is below this (gpu/row_split_chunks.py:130-142); 0 disables.
         self.k2_rows_max_r = K2_ROWS_MAX_R
@@ -615,6 +624,9 @@ class Engine:
         # The subset test has prefix subsets to look up only from K=3 on.
         classify = (infer or prune) and width >= 2
         mode = (1 if prune or infer else 0) | (2 if infer else 0)
+        deep = self._deep if (infer and self.deduction_bounds and self.fused and width + 1 <= 24) else None
+        if deep is not None:
+            mode |= 4  # ETM_SUBSET_BOUNDS
         big = sizes > self.small_group
         tensor = self.method == "tensor"
         pcnt = np.zeros(G, np.int64)
@@ -721,11 +733,20 @@ class Engine:
                         _p(gen.rows), width, gen.n, _p(gen.counts), _p(gen.free), _p(grp_first), _p(grp_size),
                         _p(cand_off), g0, g1, mode, _p(cls), _p(counts), _stream())
                 else:
+                    d2, d3, n_tot = deep if deep is not None else (None, None, n_rows)
                     fn = lambda: self.lib.etm_classify_sel(  # noqa: E731
                         _p(gen.rows), width, gen.n, _p(gen.counts), _p(gen.free), _p(grp_first), _p(grp_size),
-                        _p(cand_off), g0, g1, mode, mc, _p(cls), _p(counts), _p(bits), _stream())
+                        _p(cand_off), g0, g1, mode if sel is not None else mode & ~4, mc,
+                        _p(d2.rows) if d2 is not None else None, d2.n if d2 is not None else 0,
+                        _p(d2.counts) if d2 is not None else None, _p(d3.rows) if d3 is not None else None,
+                        d3.n if d3 is not None else 0, _p(d3.counts) if d3 is not None else None, n_tot, _p(cls),
+                        _p(counts), _p(bits), _stream())
                 check(self._launch("classify", n_c * 5, fn), "etm_classify")
                 self.launches += 1
+                if self.class_stats:
+                    by_class = torch.bincount(cls[:n_c].to(torch.int64), minlength=3).cpu().tolist()
+                    stats.n_skipped += int(by_class[1])
+                    stats.n_inferred += int(by_class[2])
             if k2_rows:
                 stats.row_wise = True
                 # K=2 from the transactions (one group of every generator): pair counts by row-wise increments.
@@ -929,6 +950,8 @@ class Engine:
         out = MineOutput(n_rows, mc, gen_cols.astype(np.int64), gen_cols.astype(np.int64),
                          col_counts[gen_cols].astype(np.int64))
         out.stats.append(LevelStats(1, n_cols, len(gen_cols), (time.perf_counter() - t0) * 1e3))
+        #: The level stats of the latest mine (the same list as its MineOutput's).
+        self.last_stats = out.stats
         if level_callback:
             level_callback(1, n_cols, len(gen_cols), out.stats[-1].ms)
         n_logical = n_cols if n_cols_logical is None else n_cols_logical
@@ -951,9 +974,12 @@ class Engine:
         gen = Level(torch.arange(ng, dtype=torch.int32, device=self.device)[:, None].contiguous(),
                     torch.from_numpy(col_counts[gen_cols].astype(np.int32)).to(self.device),
                     torch.from_numpy(free1[free1] if prune else free1).to(self.device).to(torch.uint8))
+        hist = [gen]  # complete levels 1, 2, ... (under inference without the free-set prune: every frequent set)
         k = 2
         while k <= max_k and gen.n >= k:
             t_level = time.perf_counter()
+            # Levels k-2 and k-3 for the deduction bounds of level k (k >= 3).
+            self._deep = (hist[k - 3], hist[k - 4] if k >= 4 else None, n_rows) if k >= 3 else None
             new, stats = self.count_level(gen, fbv, ldp, n_words, mc, infer, prune, n_rows)
             new = self.finish_level(new, gen, track_free, prune)
             stats.n_frequent = new.n
@@ -967,6 +993,7 @@ class Engine:
             if new.n == 0:
                 break
             out.levels.append(new)
+            hist.append(new)
             gen = new
             k += 1
         return out
@@ -975,5 +1002,6 @@ class Engine:
 def mine(bitvecs, n_rows: int, min_support: float, max_length: int | None = None, **kw) -> MineOutput:
     """Mine device bitvectors [n_cols, ceil(N/64)] with a fresh ``Engine`` (see ``Engine.mine``)."""
     engine_kw = {k: kw.pop(k) for k in ("method", "form", "chunk_cands", "small_group", "device", "project",
-                                        "proj_density", "proj_bytes", "tc_elem", "pipeline", "autotune", "fused") if k in kw}
+                                        "proj_density", "proj_bytes", "tc_elem", "pipeline", "autotune", "fused",
+                                        "deduction_bounds") if k in kw}
     return Engine(**engine_kw).mine(bitvecs, n_rows, min_support, max_length, **kw)

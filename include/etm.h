@@ -48,6 +48,10 @@ extern "C" {
 /* Mode bits of etm_classify (gpu/kernels/subset_index.py SUBSET_PRUNE / SUBSET_INFER). */
 #define ETM_SUBSET_PRUNE 1
 #define ETM_SUBSET_INFER 2
+/* With ETM_SUBSET_INFER, in etm_classify_sel: settle the candidates of at most 24 items that inference
+ * leaves by the deduction bounds of depth <= 3 (SUBSET_BOUNDS, gpu/kernels/_src/_subset_index.cu:93-136):
+ * SKIP when the upper bound is below min_count, INFER when the bounds meet. */
+#define ETM_SUBSET_BOUNDS 4
 
 /* Count methods of etm_pair_counts / etm_count_tiles. */
 #define ETM_METHOD_POPCOUNT 0 /* AND + popcount on CUDA cores */
@@ -357,7 +361,10 @@ int etm_count_tiles_split(const uint64_t* fbv, int64_t ld, int64_t n_words, cons
  * ceil(n_cands / 32) words before the chunk's first call). Of the candidates
  * a call counts, only those reaching min_count get out_counts[t] written and
  * their bit set; the other slots are left untouched. etm_classify_sel sets
- * the bit of an inferred candidate reaching min_count. Arguments otherwise as
+ * the bit of an inferred candidate reaching min_count; with ETM_SUBSET_BOUNDS
+ * in mode it also applies the deduction bounds, from the complete levels k-2
+ * (deep2: rows [deep2_n][k-2] sorted, counts) and, for k > 3, k-3 (deep3),
+ * with n_transactions the count of the empty set at k = 3. Arguments otherwise as
  * in the dense forms (etm_count_tiles with the popcount method,
  * etm_count_cands, etm_count_tiles_proj, etm_classify).
  */
@@ -378,7 +385,10 @@ int etm_count_tiles_proj_sel(const uint64_t* cbuf, const int64_t* cbase, const i
 int etm_classify_sel(const int32_t* rows, int32_t width, int64_t n_rows, const int32_t* counts,
                      const uint8_t* free_flags, const int64_t* grp_first, const int32_t* grp_size,
                      const int64_t* cand_off, int64_t g0, int64_t g1, int32_t mode, int32_t min_count,
-                     uint8_t* out_cls, int32_t* out_counts, uint32_t* surv_bits, void* stream);
+                     const int32_t* deep2_rows, int64_t deep2_n, const int32_t* deep2_counts,
+                     const int32_t* deep3_rows, int64_t deep3_n, const int32_t* deep3_counts,
+                     int64_t n_transactions, uint8_t* out_cls, int32_t* out_counts, uint32_t* surv_bits,
+                     void* stream);
 
 /*
  * Survivor bits of a chunk whose counts are dense (the row-wise kernels):

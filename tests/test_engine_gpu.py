@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from oracle import miner
-from tests.conftest import case_input
+from tests.conftest import case_input, csr_of_rows
 from tests.helpers import bitvecs_of, digest_pairs, table_of
 
 pytestmark = pytest.mark.gpu
@@ -243,3 +243,55 @@ def test_string_and_float_items_mine_like_their_integer_codes(pkg):
     floats = [[float(x) + 0.5 for x in t.items[t.indptr[r]:t.indptr[r + 1]]] for r in range(t.n_rows)]
     got_f = pkg.result_pairs(pkg.apriori(floats, min_support=0.005, use_gpu=True, warn_complexity=False), t.n_rows)
     assert sorted(got_f) == sorted((tuple(i + 0.5 for i in s), c) for s, c in want)
+
+
+@pytest.mark.parametrize("name", ["plain_small_infer", "deep_sparse_small", "implication_infer"])
+def test_deduction_bounds_settle_candidates_and_change_nothing(pkg, golden_cases, name):
+    """Under generator pruning the deduction bounds (depth <= 3) settle candidates the subset test leaves
+    (more INFER or SKIP classes), and the result is the golden one with and without them."""
+    from importlib import import_module
+
+    engm = import_module(pkg.__name__ + ".engine")
+    case = golden_cases[name]
+    indptr, items, n_rows = case_input(pkg, case)
+    settled = {}
+    for bounds in (False, True):
+        eng = engm.Engine(deduction_bounds=bounds)
+        eng.class_stats = True
+        got = pkg.apriori(table_of(indptr, items, n_rows), min_support=case["min_support"],
+                          max_length=case["max_length"], use_gpu=True, use_generator_pruning=True, engine=eng,
+                          warn_complexity=False, level_callback=lambda *a: None)
+        ref, col_items = miner.mine_transactions(indptr, items, n_rows, case["min_support"], case["max_length"],
+                                                 use_generator_pruning=True)
+        assert pkg.result_pairs(got, n_rows) == miner.canonical(ref.levels, col_items)
+        settled[bounds] = sum(s.n_inferred + s.n_skipped for s in eng_stats(got, eng))
+    assert settled[True] >= settled[False]
+
+
+def eng_stats(result, eng):
+    """The level stats of the engine's last mine (recorded by apriori's profile session)."""
+    return eng.last_stats
+
+
+def test_deduction_bounds_skip_a_candidate_inference_cannot_settle(pkg):
+    """100 rows, each holding at least one of a, b, c: 5 x {a,b,c}, 30 x {a,b}, 30 x {a,c}, 35 x {b,c}. Every
+    subset of {a,b,c} is frequent and free at min_count 10, so inference leaves it; the depth-3 upper bound
+    s(bc)+s(ac)+s(ab) - s(c)-s(b)-s(a) + N = 40+35+35 - 70-70-65 + 100 = 5 (= s(abc), as every row holds one
+    of the three) is below 10, so the bounds skip it without counting; the result stays the oracle's."""
+    import torch
+    from importlib import import_module
+
+    engm = import_module(pkg.__name__ + ".engine")
+    rows = [[0, 1, 2]] * 5 + [[0, 1]] * 30 + [[0, 2]] * 30 + [[1, 2]] * 35
+    indptr, items, n_rows = csr_of_rows(rows)
+    bv, _ = bitvecs_of(indptr, items, n_rows)
+    dev = torch.from_numpy(bv.view(np.int64)).cuda()
+    ref = miner.mine_bitvecs(bv, n_rows, 0.1, None, use_generator_pruning=True)
+    skipped = {}
+    for bounds in (False, True):
+        eng = engm.Engine(deduction_bounds=bounds)
+        eng.class_stats = True
+        out = eng.mine(dev, n_rows, 0.1, None, use_generator_pruning=True)
+        assert miner.canonical([(c, n) for c, n in out.host_levels()]) == miner.canonical(ref.levels)
+        skipped[bounds] = sum(st.n_skipped for st in out.stats)
+    assert skipped == {False: 0, True: 1}
