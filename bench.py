@@ -449,6 +449,9 @@ def deep_sparse_line(pkg, lib, steps: int, warmup: int, with_cpu: bool, cpu_budg
     return line
 
 
+TILE_PAIR_WORDS = 64 * 64  # pair counts a 64 x 64 tile-pair updates per word
+
+
 def hbm_kernel_rooflines(pkg, lib, n_rows: int = 20_000_000, reps: int = 3) -> list[dict]:
     """The AND+popcount and bitvector kernels on the deep sparse workload's shape (20M rows x 2,000 items,
     planted patterns, generated on the device): per kernel its CUDA-event time (median of ``reps`` after a
@@ -542,6 +545,24 @@ def hbm_kernel_rooflines(pkg, lib, n_rows: int = 20_000_000, reps: int = 3) -> l
         gbs = nbytes / (ms / 1e3) / 1e9
         out.append({"kernel": name, "ms": round(ms, 3), "algorithmic_bytes": int(nbytes), "bytes": how,
                     "achieved_gbs": round(gbs, 1), "peak_gbs": peak, "frac": round(gbs / peak, 3)})
+    # The tile kernel is bound by the popcount pipe (64 x 64 pair counts per staged word pair), so its roofline is
+    # the measured AND+popcount issue rate of its inner loop; the HBM fraction above is only its input stream.
+    import ctypes
+
+    rate = ctypes.c_double(0.0)
+    if lib.etm_popc_rate(1 << 14, ctypes.byref(rate), st) != 0:
+        raise RuntimeError(lib.etm_last_error().decode())
+    tiles = next(r for r in out if r["kernel"] == "count_tiles")
+    useful = m_t * (m_t - 1) // 2 * n_words
+    issued = n_tp * TILE_PAIR_WORDS * n_words
+    gops = useful / (tiles["ms"] / 1e3) / 1e9
+    tiles.update({"bound": "popc", "pair_words": useful, "issued_pair_words": issued,
+                  "achieved_gops": round(gops, 1), "popc_peak_gops": round(rate.value, 1),
+                  "frac_popc": round(gops / rate.value, 3),
+                  "frac_popc_issued": round(issued / (tiles["ms"] / 1e3) / 1e9 / rate.value, 3),
+                  "peak_source": "measured: etm_popc_rate (the tile kernel's 4 x 4 AND+popcount block on every SM)"})
+    for r in out:
+        r.setdefault("bound", "hbm")
     # The outputs agree with each other: K=1 counts of the rebuilt bitvectors equal those of the originals.
     assert torch.equal(out_bv, bvi), "build_bitvecs does not reproduce the generator's bitvectors"
     del bv, bvi, out_bv, fbv, ids, row_ptr
@@ -674,6 +695,10 @@ def main() -> None:
     ap.add_argument("--ref-budget", type=float, default=None,
                     help="reference arm: seconds each step's mine may run (default: 180 / steps, within 20..90)")
     ap.add_argument("--no-side", action="store_true", help="skip the plain small and deep sparse side workloads")
+    ap.add_argument("--no-serial", action="store_true", help="skip the one-stream mine that gives per-kernel times")
+    ap.add_argument("--no-hbm", action="store_true", help="skip the AND+popcount / bitvector kernel rooflines")
+    ap.add_argument("--hbm-rows-default", type=int, default=8_000_000,
+                    help="transactions of the kernel-roofline input in the default line")
     ap.add_argument("--no-pipeline", action="store_true",
                     help="project and count chunks in turn on one stream (per-kernel times without overlap)")
     args = ap.parse_args()
@@ -775,6 +800,29 @@ def main() -> None:
         assert [s.n_frequent for s in po.stats] == ref_sizes
         plain = {"value": plain_s, "unit": "s", "speedup_batched": plain_s / (ms / 1e3)}
 
+    # Serial kernel times: one mine on one stream (the projection not overlapped with the Gram), so every
+    # kernel's CUDA-event time is its own and the per-kernel rates are not mixed across streams.
+    serial = None
+    if not args.no_serial:
+        se = engm.Engine(form="batched", method=method, tc_elem=args.tc_elem, proj_bytes=int(args.proj_gb * (1 << 30)),
+                         pipeline=False, **extra)
+        se.profile_kernels = True
+        one(se)
+        se.reset_kernel_times()
+        torch.cuda.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        so = one(se)
+        s1.record()
+        torch.cuda.synchronize()
+        assert [s.n_frequent for s in so.stats] == ref_sizes
+        sk = se.kernel_report()
+        serial = {"ms_per_step": s0.elapsed_time(s1), "launches": sum(r["launches"] for r in sk.values()),
+                  "kernels": {n: {"launches": r["launches"], "ms": round(r["ms"], 2), "gbs": round(r["gbs"], 1),
+                                  "tflops": round(r["tflops"], 1) if r["flops"] else None}
+                              for n, r in sorted(sk.items(), key=lambda kv: -kv[1]["ms"])}}
+        del se, so
+
     # End to end through the public API: pinned host bitvectors in, itemsets out.
     host = torch.empty(bv.shape, dtype=torch.int64, pin_memory=True)
     host.copy_(bv.view(torch.int64))
@@ -863,6 +911,14 @@ def main() -> None:
     if rank == 0 and world == 1 and not args.no_side:
         side.append(transactions_line(pkg, "plain_small_tx", max(3, args.steps), 3, with_cpu=not args.no_cpu))
         side.append(deep_sparse_line(pkg, lib, max(2, args.steps), 2, with_cpu=not args.no_cpu))
+    # The AND+popcount and bitvector kernels against the HBM copy peak (the tile kernel against the popcount
+    # pipe), on the deep sparse workload's shape with fewer rows.
+    rooflines = None
+    if rank == 0 and not args.no_hbm:
+        out.levels.clear()
+        torch.cuda.empty_cache()
+        rooflines = {"rows": args.hbm_rows_default, "items": 2_000,
+                     "kernels": hbm_kernel_rooflines(pkg, lib, n_rows=args.hbm_rows_default)}
 
     if rank == 0:
         line = {
@@ -882,6 +938,8 @@ def main() -> None:
             "e2e": {"value": statistics.median(e2e_ms) / 1e3, "unit": "s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "itemsets": n_items_out},
             "roofline": roof,
+            "rooflines": rooflines,
+            "serial": serial,
             "kernels": kern,
             "cpu_baseline": cpu,
             "workloads": side,

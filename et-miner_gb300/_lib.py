@@ -111,6 +111,7 @@ SIGNATURES: dict[str, tuple] = {
                                               _P, _P, _P]),
     "etm_gram_block_members": (ctypes.c_int, [_I32]),
     "etm_tc_mma_rate": (ctypes.c_int, [_I32, _I64, ctypes.POINTER(_D), _P]),
+    "etm_popc_rate": (ctypes.c_int, [_I64, ctypes.POINTER(_D), _P]),
     "etm_set_wait_limits": (ctypes.c_int, [_I64, _I64]),
     "etm_device_status": (ctypes.c_int, [_P]),
     "etm_level_compact": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _P, _P, _P, _I64, _I64, _I32, _P, _P, _I64, _P, _P, _I64, _P]),

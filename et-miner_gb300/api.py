@@ -29,14 +29,17 @@ from __future__ import annotations
 
 import math
 import numbers
+import os
 import time
 import warnings
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 from math import comb
 from typing import Any
 
 import numpy as np
 
+from . import flush as _flush
 from .engine import Engine, MineOutput, min_count
 
 try:  # optional: results come back as polars frames when it is installed
@@ -452,6 +455,96 @@ def _emit(out: MineOutput, col_items: np.ndarray, labels: np.ndarray | None = No
     return frame
 
 
+class _LevelFlush:
+    """The per-level parquet flush (``io/flush.py:63-140`` driven from ``gpu/row_split.py:511-535``): each
+    final level goes to ``frequent_k{k}.parquet`` on a writer thread while the device counts the next
+    one. At most two levels wait for the writer; ``close`` waits for every write and raises its error."""
+
+    def __init__(self, output_dir: str, item_of_col: np.ndarray, n_rows: int):
+        self.dir = output_dir
+        self.items = item_of_col
+        self.n = max(1, n_rows)
+        self.pool = ThreadPoolExecutor(1, thread_name_prefix="etm-flush")
+        self.pending: list = []
+
+    def __call__(self, k: int, cols: np.ndarray, counts: np.ndarray) -> None:
+        while len(self.pending) >= 2:
+            self.pending.pop(0).result()
+        items = self.items[cols]
+        sup = counts.astype(np.float64) / self.n
+        self.pending.append(self.pool.submit(_flush.write_level, _flush.level_path(self.dir, k), items, sup))
+
+    def close(self) -> None:
+        try:
+            for f in self.pending:
+                f.result()
+        finally:
+            self.pending = []
+            self.pool.shutdown(wait=True)
+
+
+def _check_flush_options(output_dir, resume_from_k) -> bool:
+    """Validate output_dir / resume_from_k; True when the mine resumes (``gpu/row_split.py:540``: K >= 2 with
+    an output directory; resume_from_k=1 mines from the start)."""
+    if output_dir is not None:
+        if not isinstance(output_dir, (str, os.PathLike)):
+            raise TypeError(f"output_dir must be a path, got {type(output_dir).__name__}")
+        if "://" in os.fspath(output_dir):
+            raise ValueError(f"output_dir={output_dir!r}: only a local directory is supported (no object-store upload)")
+    if resume_from_k is None:
+        return False
+    if isinstance(resume_from_k, bool) or not isinstance(resume_from_k, numbers.Integral) or resume_from_k < 1:
+        raise ValueError(f"resume_from_k must be a positive integer, got {resume_from_k!r}")
+    if output_dir is None:
+        raise ValueError("resume_from_k needs output_dir: the level to resume from is read from "
+                         "output_dir/frequent_k{resume_from_k}.parquet")
+    return resume_from_k >= 2
+
+
+def _resume_level(output_dir: str, k: int, item_of_col: np.ndarray, n_rows: int):
+    """(k, caller columns [n, k], counts [n]) of the flushed level k: item ids map to columns, counts come back
+    as rint(support * N), exact for any int32 count (``gpu/row_split.py:546-606``)."""
+    path = _flush.level_path(output_dir, k)
+    if not path.exists():
+        raise FileNotFoundError(f"resume_from_k={k}: {path} does not exist")
+    itemsets, sup = _flush.read_level(path)
+    if len(sup) and itemsets.shape[1] != k:
+        raise ValueError(f"{path} holds itemsets of length {itemsets.shape[1]}, not {k}")
+    flat = itemsets.reshape(-1)
+    order = np.argsort(item_of_col, kind="stable")
+    ids = item_of_col[order]
+    if flat.size:
+        if item_of_col.dtype == np.uint64:
+            if flat.dtype.kind == "i" and (flat < 0).any():
+                raise ValueError(f"{path} holds item ids that are not in this input")
+            flat = flat.astype(np.uint64)
+        else:
+            flat = flat.astype(np.int64)
+        pos = np.minimum(np.searchsorted(ids, flat), max(0, len(ids) - 1))
+        if len(ids) == 0 or (ids[pos] != flat).any():
+            raise ValueError(f"{path} holds item ids that are not in this input")
+        cols = order[pos].astype(np.int64).reshape(-1, k)
+    else:
+        cols = np.zeros((0, k), np.int64)
+    counts = np.rint(sup.astype(np.float64) * n_rows).astype(np.int64)
+    return k, cols, counts
+
+
+def _mine_to(eng: Engine, bv, n_rows: int, min_support: float, max_length, item_of_col: np.ndarray,
+             output_dir, resume_from_k, **kw) -> MineOutput:
+    """One mine, with the per-level flush and resume when output_dir is given."""
+    if output_dir is None:
+        return eng.mine(bv, n_rows, min_support, max_length, **kw)
+    os.makedirs(output_dir, exist_ok=True)
+    resume = _resume_level(output_dir, int(resume_from_k), item_of_col, n_rows) if resume_from_k else None
+    writer = _LevelFlush(os.fspath(output_dir), item_of_col, n_rows)
+    try:
+        return eng.mine(bv, n_rows, min_support, max_length, on_level=writer, resume=resume, keep_levels=False,
+                        **kw)
+    finally:
+        writer.close()
+
+
 def _session_from(out: MineOutput, session: ProfilingSession) -> None:
     for s in out.stats:
         session.record_phase(f"k{s.k}", s.ms, n_candidates=s.n_candidates, n_frequent=s.n_frequent,
@@ -504,16 +597,15 @@ def apriori(
         raise ValueError("gpu_resident was removed: use_gpu=True (or bitvecs=) keeps candidates and counts on the GPU.")
     _unsupported(
         streaming=(streaming, "SON streaming is not this engine's path"),
-        output_dir=(output_dir is not None, "the per-level parquet flush is not built"),
-        resume_from_k=(resume_from_k is not None, "resume is not built"),
         anchor_items=(anchor_items is not None, "anchor filtering is not built"),
         memory_budget_gb=(memory_budget_gb is not None, "it only sizes SON chunks"),
         n_gpus=(n_gpus != 1, "one GB300 per call; run independent calls per GPU"),
     )
     if bitvecs is None and not use_gpu:
         raise ValueError("the GB300 engine serves the GPU route: pass use_gpu=True or bitvecs=")
+    resuming = _check_flush_options(output_dir, resume_from_k)
+    resume_k = resume_from_k if resuming else None
     session = ProfilingSession() if profile else None
-    eng = engine or Engine()
 
     if bitvecs is not None:
         if transactions is not None:
@@ -541,13 +633,16 @@ def apriori(
         vals = [int(col_to_item[c]) for c in range(shape[0])] if shape[0] else []
         wide = any(v > np.iinfo(np.int64).max for v in vals)
         col_items = np.array(vals, dtype=np.uint64 if wide else np.int64)
-        out = eng.mine(bv, n_trans, min_support, max_length, prune_equal_support=prune_equal_support,
-                       use_generator_pruning=use_generator_pruning, level_callback=level_callback,
+        eng = engine or Engine()
+        out = _mine_to(eng, bv, n_trans, min_support, max_length, col_items, output_dir, resume_k,
+                       prune_equal_support=prune_equal_support, use_generator_pruning=use_generator_pruning,
+                       level_callback=level_callback,
                        n_cols_logical=(max(col_to_item.keys()) + 1) if col_to_item else 0,
                        max_ram_gb=max_ram_gb, max_vram_gb=max_vram_gb)
         if warn_complexity and out.stats:
             _warn_complexity(out.stats[0].n_frequent, min_support)
-        df = _emit(out, col_items)
+        # With output_dir the levels are in the files; the frame is empty (gpu/row_split.py:1172-1178).
+        df = _emit(out, col_items) if output_dir is None else _frame([], max(1, n_trans), wide)
         if session is not None:
             _session_from(out, session)
         return (df, session) if profile else df
@@ -555,6 +650,9 @@ def apriori(
     if transactions is None:
         raise ValueError("Either 'transactions' or 'bitvecs' must be provided")
     indptr, flat, kind, labels = _list_column(transactions, item_col)
+    if labels is not None and (output_dir is not None or resume_from_k is not None):
+        raise ValueError("output_dir and resume_from_k store integer item ids: these items are not integer ids")
+    eng = engine or Engine()
     n_rows = len(indptr) - 1
     if n_rows > np.iinfo(np.int32).max:
         raise ValueError(f"n_transactions={n_rows:,} exceeds int32 max")
@@ -568,12 +666,13 @@ def apriori(
     rows = (row_ptr, cols, row_len)
     max_tx = int(np.diff(indptr).max()) if n_rows else 0
     eff = min(max_length, max_tx) if max_length else max_tx
-    out = eng.mine(bv, n_rows, min_support, eff if eff >= 1 else 1, prune_equal_support=prune_equal_support,
-                   use_generator_pruning=use_generator_pruning, level_callback=level_callback, rows=rows,
-                   max_ram_gb=max_ram_gb, max_vram_gb=max_vram_gb)
+    col_items = items.astype(np.uint64 if wide else np.int64)
+    out = _mine_to(eng, bv, n_rows, min_support, eff if eff >= 1 else 1, col_items, output_dir, resume_k,
+                   prune_equal_support=prune_equal_support, use_generator_pruning=use_generator_pruning,
+                   level_callback=level_callback, rows=rows, max_ram_gb=max_ram_gb, max_vram_gb=max_vram_gb)
     if warn_complexity and out.stats:
         _warn_complexity(out.stats[0].n_frequent, min_support)
-    df = _emit(out, items.astype(np.uint64 if wide else np.int64), labels)
+    df = _emit(out, col_items, labels) if output_dir is None else _frame([], max(1, n_rows), wide)
     if session is not None:
         _session_from(out, session)
     return (df, session) if profile else df

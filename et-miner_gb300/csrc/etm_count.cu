@@ -353,3 +353,74 @@ extern "C" int etm_count_cands_sel(const uint64_t* fbv, int64_t ld, int64_t n_wo
     ETM_LAUNCHED("count_cands");
     return ETM_OK;
 }
+
+namespace {
+
+// The AND+popcount issue rate of the tile kernel's inner loop with nothing else in the way: every thread
+// keeps a 4 x 4 block of counters over 4 + 4 words in registers and adds popc(a_r & b_c) per pair, the
+// operands rotating every step so no product can be hoisted. The rate is the CUDA-core roofline of the
+// tile kernels (their pair counts per second), which are bound by the popcount pipe, not by HBM.
+constexpr int RATE_THREADS = 256;
+
+__global__ void __launch_bounds__(RATE_THREADS) popc_rate_kernel(int64_t iters, unsigned* __restrict__ sink) {
+    const uint64_t seed = 0x9E3779B97F4A7C15ULL * (uint64_t)(blockIdx.x * RATE_THREADS + threadIdx.x + 1);
+    uint64_t a[4], b[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        a[r] = seed ^ (0xD6E8FEB86659FD93ULL * (uint64_t)(r + 1));
+        b[r] = seed + (0xA0761D6478BD642FULL * (uint64_t)(r + 5));
+    }
+    unsigned acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[r][c] = 0;
+    for (int64_t it = 0; it < iters; it++) {
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) acc[r][c] += __popcll(a[r] & b[c]);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            a[r] = (a[r] << 1) | (a[r] >> 63);
+            b[r] += 0x9E3779B97F4A7C15ULL;
+        }
+    }
+    unsigned total = 0;
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) total += acc[r][c];
+    if (total == 0xFFFFFFFFu) sink[0] = total;  // never true in practice; keeps the loop alive
+}
+
+}  // namespace
+
+extern "C" int etm_popc_rate(int64_t iters, double* out_gops, void* stream) {
+    ETM_REQUIRE(iters > 0 && iters < (1LL << 32) && out_gops != nullptr, ETM_EINVAL, "etm_popc_rate: bad iters");
+    cudaStream_t s = as_stream(stream);
+    unsigned* sink = nullptr;
+    ETM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&sink), sizeof(unsigned), s));
+    const int grid = max(1, sm_count()) * 8;
+    cudaEvent_t e0, e1;
+    ETM_CUDA(cudaEventCreate(&e0));
+    ETM_CUDA(cudaEventCreate(&e1));
+    popc_rate_kernel<<<grid, RATE_THREADS, 0, s>>>(iters / 8 + 1, sink);  // warm-up
+    cudaEventRecord(e0, s);
+    popc_rate_kernel<<<grid, RATE_THREADS, 0, s>>>(iters, sink);
+    cudaEventRecord(e1, s);
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (err == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeAsync(sink, s);
+    if (err != cudaSuccess) {
+        etm::set_error("etm_popc_rate: %s", cudaGetErrorString(err));
+        return ETM_ECUDA;
+    }
+    const double ops = 16.0 * (double)iters * (double)grid * RATE_THREADS;
+    *out_gops = ms > 0.f ? ops / (ms * 1e-3) / 1e9 : 0.0;
+    return ETM_OK;
+}

@@ -922,7 +922,7 @@ class Engine:
     def mine(self, bitvecs, n_rows: int, min_support: float, max_length: int | None = None, *,
              prune_equal_support: bool = False, use_generator_pruning: bool = False,
              level_callback=None, n_cols_logical: int | None = None, rows=None, max_ram_gb: float | None = None,
-             max_vram_gb: float | None = None) -> MineOutput:
+             max_vram_gb: float | None = None, on_level=None, resume=None, keep_levels: bool = True) -> MineOutput:
         """Mine device bitvectors. ``rows`` = (row_ptr int64, cols int32, host row lengths) on the device,
         the transactions the bitvectors were built from, lets K=2 count row-wise when its rows are short
         against the pair space (the reference's rule, gpu/row_split_chunks.py:124-142).
@@ -930,6 +930,14 @@ class Engine:
         ``max_ram_gb`` / ``max_vram_gb``: after every level, the process's resident memory and the device
         memory allocated through torch (every engine buffer) are checked against them; over a limit the mine raises
         MemoryError instead of returning a partial lattice (gpu/row_split.py:467-487).
+
+        ``on_level(k, caller_cols int64 [n, k], counts int64 [n])`` receives every emitted level on the host
+        as soon as it is final (the per-level flush); with ``keep_levels=False`` the emitted levels are not kept
+        in the output (only the few the next levels need stay on the device).
+
+        ``resume = (k, caller_cols [n, k], counts [n])``: start from a complete emitted level k read back from a
+        flush (gpu/row_split.py:546-606): levels 1..k are neither counted nor emitted again; the first resumed
+        level has no free flags to infer from, and the deduction bounds wait for levels k-2 and k-3.
         """
         ptr, (n_cols, ld), _owner = as_device_bitvecs(bitvecs)
         self._k2_rows = None
@@ -947,16 +955,22 @@ class Engine:
         freq = np.flatnonzero(col_counts >= mc)
         free1 = col_counts[freq] < n_rows
         gen_cols = freq[free1] if prune else freq
-        out = MineOutput(n_rows, mc, gen_cols.astype(np.int64), gen_cols.astype(np.int64),
-                         col_counts[gen_cols].astype(np.int64))
+        r_k = int(resume[0]) if resume is not None else 0
+        if resume is not None:
+            out = MineOutput(n_rows, mc, gen_cols.astype(np.int64), np.zeros(0, np.int64), np.zeros(0, np.int64))
+        else:
+            out = MineOutput(n_rows, mc, gen_cols.astype(np.int64), gen_cols.astype(np.int64),
+                             col_counts[gen_cols].astype(np.int64))
         out.stats.append(LevelStats(1, n_cols, len(gen_cols), (time.perf_counter() - t0) * 1e3))
         #: The level stats of the latest mine (the same list as its MineOutput's).
         self.last_stats = out.stats
-        if level_callback:
+        if level_callback and resume is None:
             level_callback(1, n_cols, len(gen_cols), out.stats[-1].ms)
+        if on_level is not None and resume is None and len(gen_cols):
+            on_level(1, gen_cols[:, None].astype(np.int64), col_counts[gen_cols].astype(np.int64))
         n_logical = n_cols if n_cols_logical is None else n_cols_logical
         max_k = min(max_length if max_length else n_logical, n_logical)
-        if len(gen_cols) < 2 or max_k < 2:
+        if len(gen_cols) < 2 or max_k < max(2, r_k + 1):
             return out
         fbv, ldp = self.gather(ptr, ld, gen_cols, n_words)
         ng = len(gen_cols)
@@ -969,18 +983,35 @@ class Engine:
             self._rows_input = dict(rp=rp, cl=cl, nnz=int(cl.numel()), lut=lut, n_r=int(rp.numel()) - 1,
                                     pair_work=pair_work, ng=ng)
             r = pair_work / max(1.0, ng * (ng - 1) / 2 * n_words)
-            if self.k2_rows_max_r > 0 and r < self.k2_rows_max_r:
+            if self.k2_rows_max_r > 0 and r < self.k2_rows_max_r and resume is None:
                 self._k2_rows = (rp, cl, int(cl.numel()), lut, int(rp.numel()) - 1)
-        gen = Level(torch.arange(ng, dtype=torch.int32, device=self.device)[:, None].contiguous(),
-                    torch.from_numpy(col_counts[gen_cols].astype(np.int32)).to(self.device),
-                    torch.from_numpy(free1[free1] if prune else free1).to(self.device).to(torch.uint8))
-        hist = [gen]  # complete levels 1, 2, ... (under inference without the free-set prune: every frequent set)
-        k = 2
+        if resume is None:
+            gen = Level(torch.arange(ng, dtype=torch.int32, device=self.device)[:, None].contiguous(),
+                        torch.from_numpy(col_counts[gen_cols].astype(np.int32)).to(self.device),
+                        torch.from_numpy(free1[free1] if prune else free1).to(self.device).to(torch.uint8))
+            # Complete levels 1, 2, ... (under inference without the free-set prune: every frequent set).
+            hist: list[Level | None] = [gen]
+            k = 2
+        else:
+            cols_r = np.asarray(resume[1], np.int64)
+            counts_r = np.asarray(resume[2], np.int64)
+            gidx = np.searchsorted(gen_cols, cols_r)
+            if cols_r.size and (gidx.max() >= ng or (gen_cols[np.minimum(gidx, ng - 1)] != cols_r).any()):
+                raise ValueError(f"the level-{r_k} itemsets to resume from hold items that are not frequent here")
+            order = np.lexsort(gidx.T[::-1]) if gidx.size else np.zeros(0, np.int64)
+            gen = Level(torch.from_numpy(np.ascontiguousarray(gidx[order], dtype=np.int32)).to(self.device),
+                        torch.from_numpy(counts_r[order].astype(np.int32)).to(self.device), None)
+            hist = [None] * (r_k - 1) + [gen]  # levels 1..k-1 are not at hand: no bounds until three follow
+            k = r_k + 1
         while k <= max_k and gen.n >= k:
             t_level = time.perf_counter()
-            # Levels k-2 and k-3 for the deduction bounds of level k (k >= 3).
-            self._deep = (hist[k - 3], hist[k - 4] if k >= 4 else None, n_rows) if k >= 3 else None
-            new, stats = self.count_level(gen, fbv, ldp, n_words, mc, infer, prune, n_rows)
+            # Levels k-2 and k-3 for the deduction bounds of level k (k >= 3), when both are at hand.
+            d2 = hist[k - 3] if k >= 3 else None
+            d3 = hist[k - 4] if k >= 4 else None
+            self._deep = (d2, d3, n_rows) if d2 is not None and (k == 3 or d3 is not None) else None
+            # The first resumed level has no free flags: inference waits one level.
+            level_infer = infer and gen.free is not None
+            new, stats = self.count_level(gen, fbv, ldp, n_words, mc, level_infer, prune, n_rows)
             new = self.finish_level(new, gen, track_free, prune)
             stats.n_frequent = new.n
             stats.ms = (time.perf_counter() - t_level) * 1e3
@@ -992,10 +1023,16 @@ class Engine:
                                    max_ram_gb, max_vram_gb)
             if new.n == 0:
                 break
-            out.levels.append(new)
+            if on_level is not None:
+                on_level(k, out.gen_cols[new.rows.cpu().numpy()], new.counts.cpu().numpy().astype(np.int64))
+            if keep_levels:
+                out.levels.append(new)
             hist.append(new)
+            if len(hist) > 4:
+                hist[-5] = None  # the bounds read at most three levels back
             gen = new
             k += 1
+        self._deep = None
         return out
 
 

@@ -149,7 +149,7 @@ def check_mine(out: MineOutput, bv: torch.Tensor, n_rows: int, *, prune: bool = 
         # Extensions by a larger frequent item.
         ext_checked = ext_freq = ext_bad = 0
         if max_length is None or k + 1 <= max_length:
-            last = s_rows[:, -1]
+            last = s_rows[:, -1].contiguous()
             u = torch.rand(len(pick), generator=rng).to(dev)
             lo = torch.searchsorted(freq_items, last, right=True)
             n_larger = len(freq_items) - lo

@@ -322,6 +322,16 @@ int etm_gram_block_members(int32_t elem);
 int etm_tc_mma_rate(int32_t elem, int64_t iters, double* out_tflops, void* stream);
 
 /*
+ * AND+popcount rate of the tile kernels' inner loop, in 10^9 popc(a & b) pair
+ * words per second: 8 CTAs per SM of 256 threads, each adding popc(a_r & b_c)
+ * for a 4 x 4 register block `iters` times (timed with CUDA events on
+ * `stream`, synchronized). The roofline of etm_count_tiles* on words that stay
+ * in shared memory: those kernels are bound by the popcount pipe, not by HBM.
+ * No counterpart in the reference.
+ */
+int etm_popc_rate(int64_t iters, double* out_gops, void* stream);
+
+/*
  * Reads and clears the device status words the tensor-core kernels and the
  * projection (its bulk copies) raise when a bounded wait gives up
  * (synchronizes `stream`). Returns 0, ETM_ETIMEOUT (the kernel gave up and

@@ -45,7 +45,8 @@ def test_device_frequent_csr_matches_host(pkg, wide, mc):
     (dict(min_support=0.1, sparse_from_k=3), ValueError, "sparse_from_k"),
     (dict(min_support=0.1, prune_apriori=False), ValueError, "prune_apriori"),
     (dict(min_support=0.1, streaming=True), ValueError, "streaming"),
-    (dict(min_support=0.1, output_dir="/tmp/x"), ValueError, "output_dir"),
+    (dict(min_support=0.1, output_dir="gs://bucket/run"), ValueError, "local directory"),
+    (dict(min_support=0.1, resume_from_k=2), ValueError, "needs output_dir"),
     (dict(min_support=0.1, anchor_items={1}), ValueError, "anchor_items"),
 ])
 def test_parameter_checks_need_no_gpu(pkg, kw, exc, match):
