@@ -57,13 +57,15 @@ WORKLOADS = {
 
 
 #: DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic byte of a kernel, from one ncu
-#: capture of every launch of the 1M x 2048 dense K=2 workload (ncu --metrics dram__bytes_read.sum,
-#: dram__bytes_write.sum,gpu__time_duration.sum --clock-control none -k "regex:gram_wide_kernel|project_seg_kernel"
-#: python bench.py --workload dense_k2_mid --steps 1 --warmup 1 --no-plain --no-cpu --proj-gb 1
-#: --chunk-cands 134217728: per mine
-#: 16.21 GB against 12.66 GB for the Gram, 19.63 GB against 170.35 GB for the projection); the roofline's
-#: ``traffic`` scales it to the bench's own launches by their algorithmic bytes.
-DRAM_PER_ALGORITHMIC_BYTE = {"gram_tc": 16.21 / 12.66, "project": 19.63 / 170.35}
+#: capture of every Gram and projection launch of the 1M x 2048 dense K=2 workload (four mines: warm-up,
+#: timed step, two end-to-end calls):
+#:   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none
+#:       -k "regex:gram_kernel|project_seg" python bench.py --workload dense_k2_mid --steps 1 --warmup 1
+#:       --no-plain --no-cpu --no-side --no-serial --no-hbm --no-pipeline
+#: per mine 15.91 GB against 12.66 GB for the Gram, 14.62 GB against 170.84 GB for the projection (its column
+#: re-reads stay in L2); the roofline's ``traffic`` scales it to the bench's own launches by their
+#: algorithmic bytes.
+DRAM_PER_ALGORITHMIC_BYTE = {"gram_tc": 15.906 / 12.659, "project": 14.624 / 170.836}
 
 
 def _peaks() -> dict:

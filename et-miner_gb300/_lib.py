@@ -105,6 +105,9 @@ SIGNATURES: dict[str, tuple] = {
     "etm_prefix_segments": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _I64, _P, _P, _P]),
     "etm_project": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "etm_project_blocked": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _I64, _P, _P, _P, _I64, _P, _P, _P]),
+    "etm_rows_transpose": (ctypes.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P]),
+    "etm_project_rows": (ctypes.c_int, [_P, _I64, _I64, _P, _I64, _P, _I32, _P, _P, _P, _I64, _P, _P, _P, _I64, _P,
+                                        _P]),
     "etm_count_tiles_proj": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P]),
     "etm_count_tiles_tc": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _P, _I32, _P, _P, _P]),
     "etm_count_tiles_tc_sel": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _P, _I32, _I32, _P,

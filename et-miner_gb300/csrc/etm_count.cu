@@ -361,6 +361,7 @@ namespace {
 // operands rotating every step so no product can be hoisted. The rate is the CUDA-core roofline of the
 // tile kernels (their pair counts per second), which are bound by the popcount pipe, not by HBM.
 constexpr int RATE_THREADS = 256;
+__device__ unsigned g_popc_sink;
 
 __global__ void __launch_bounds__(RATE_THREADS) popc_rate_kernel(int64_t iters, unsigned* __restrict__ sink) {
     const uint64_t seed = 0x9E3779B97F4A7C15ULL * (uint64_t)(blockIdx.x * RATE_THREADS + threadIdx.x + 1);
@@ -400,7 +401,7 @@ extern "C" int etm_popc_rate(int64_t iters, double* out_gops, void* stream) {
     ETM_REQUIRE(iters > 0 && iters < (1LL << 32) && out_gops != nullptr, ETM_EINVAL, "etm_popc_rate: bad iters");
     cudaStream_t s = as_stream(stream);
     unsigned* sink = nullptr;
-    ETM_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&sink), sizeof(unsigned), s));
+    ETM_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&sink), g_popc_sink));
     const int grid = max(1, sm_count()) * 8;
     cudaEvent_t e0, e1;
     ETM_CUDA(cudaEventCreate(&e0));
@@ -415,7 +416,6 @@ extern "C" int etm_popc_rate(int64_t iters, double* out_gops, void* stream) {
     if (err == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    cudaFreeAsync(sink, s);
     if (err != cudaSuccess) {
         etm::set_error("etm_popc_rate: %s", cudaGetErrorString(err));
         return ETM_ECUDA;

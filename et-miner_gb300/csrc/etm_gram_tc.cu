@@ -361,10 +361,11 @@ __global__ void __launch_bounds__(STAGED ? ST_THREADS : THREADS, 1) gram_kernel(
         if (tid < 256) {
             const int64_t ia = a0 + tid, ib = b0 + tid;
             // Row-major rows: member i at cbase + i cld. Blocked rows (blocks of T members stored 4-word chunk
-            // by chunk, so a stage's words of one block are one run): member i at cbase + (i / T) T cld + 4 (i % T).
+            // by chunk, each chunk as two 2-word halves, so a stage's words of one block are one run): member i
+            // at cbase + (i / T) T cld + 2 (i % T).
             const int64_t cw = cld[wi];
-            off_a[tid] = tid < T && ia < m ? cbase[wi] + (blocked ? ua * T * cw + 4 * tid : ia * cw) : -1;
-            off_b[tid] = tid < T && ib < m ? cbase[wi] + (blocked ? ub * T * cw + 4 * tid : ib * cw) : -1;
+            off_a[tid] = tid < T && ia < m ? cbase[wi] + (blocked ? ua * T * cw + 2 * tid : ia * cw) : -1;
+            off_b[tid] = tid < T && ib < m ? cbase[wi] + (blocked ? ub * T * cw + 2 * tid : ib * cw) : -1;
         }
         int any = cls == nullptr;
         if (!any && tid < T) {
@@ -387,9 +388,10 @@ __global__ void __launch_bounds__(STAGED ? ST_THREADS : THREADS, 1) gram_kernel(
             const int hrow = is_b ? prow : prow % TH;
             if constexpr (STAGED) {
                 // Raw bits from the loader's ring (A block at 0, B block at RAW_BLOCK of a slot): wait for the
-                // slot, read this row's 32 bytes, release the slot, then expand into the operand stage.
+                // slot, read this row's two 16-byte halves (words 0-1 at 16 prow, words 2-3 at 16 (T + prow):
+                // a warp reads two contiguous 512-byte runs), release the slot, then expand into the stage.
                 const bool skip = idle || (is_b ? b0 : a0) + prow >= m;
-                const int raw_off = (is_b ? RAW_BLOCK : 0) + prow * 32;
+                const int raw_off = (is_b ? RAW_BLOCK : 0) + prow * 16;
                 for (int64_t s = 0; s < n_stages; s++) {
                     const int64_t G = gstage + s;
                     const int rs = (int)(G % RAW_STAGES);
@@ -400,7 +402,7 @@ __global__ void __launch_bounds__(STAGED ? ST_THREADS : THREADS, 1) gram_kernel(
                     uint64_t x[4] = {0, 0, 0, 0};
                     if (!skip) {
                         const uint4* r = reinterpret_cast<const uint4*>(raw + rs * RAW_SLOT + raw_off);
-                        const uint4 v0 = r[0], v1 = r[1];
+                        const uint4 v0 = r[0], v1 = r[T];
                         x[0] = (uint64_t)v0.x | ((uint64_t)v0.y << 32);
                         x[1] = (uint64_t)v0.z | ((uint64_t)v0.w << 32);
                         x[2] = (uint64_t)v1.x | ((uint64_t)v1.y << 32);
@@ -423,7 +425,7 @@ __global__ void __launch_bounds__(STAGED ? ST_THREADS : THREADS, 1) gram_kernel(
                     for (int q = 0; q < BW; q += 2) {
                         const int64_t w = s0 * WORDS + q;
                         ulonglong2 v = make_ulonglong2(0, 0);
-                        const int64_t at = off + (blocked ? (w >> 2) * (4 * T) + (w & 3) : w);
+                        const int64_t at = off + (blocked ? (w >> 2) * (4 * T) + ((w >> 1) & 1) * (2 * T) + (w & 1) : w);
                         if (off >= 0 && w + 1 < lim) v = __ldg(reinterpret_cast<const ulonglong2*>(src + at));
                         else if (off >= 0 && w < lim) v.x = __ldg(src + at);
                         x[q] = v.x;
@@ -538,7 +540,10 @@ __global__ void __launch_bounds__(STAGED ? ST_THREADS : THREADS, 1) gram_kernel(
                 }
                 mma_commit(&empty_bar[slot]);
             }
-            mma_commit(&acc_bar);
+            // A block pair without stages (an empty prefix) issues no MMA and commits nothing: its producers do
+            // not wait for the accumulator, and acc_bar's phases stay one per block pair with stages, so a
+            // later pair's epilogue can never take an earlier phase for its own.
+            if (n_stages > 0) mma_commit(&acc_bar);
         } else if (STAGED && warp == LOAD_WARP && lane == 0) {
             // ---- loader: the raw chunk of block ua (unless diagonal) and of block ub for every stage ----
             const int64_t cw = cld[wi];
@@ -556,7 +561,7 @@ __global__ void __launch_bounds__(STAGED ? ST_THREADS : THREADS, 1) gram_kernel(
             }
         }
         gstage += n_stages;
-        tile_iter += 1;
+        if (n_stages > 0) tile_iter += 1;  // one acc_bar phase per block pair with stages
         __syncthreads();
         if (*abort_flag) break;
     }
@@ -847,6 +852,8 @@ extern "C" int etm_device_status(void* stream) {
                        v, p);
     else if (v != 0)
         etm::set_error("a tensor-core counting kernel gave up a bounded wait (status %d)", v);
+    else if (p == ETM_EINVAL)
+        etm::set_error("the row-major projection met a member column past its row-major copy (status %d)", p);
     else if (p != 0)
         etm::set_error("the projection gave up a bounded wait for its bulk copies (status %d)", p);
     return v != 0 ? v : p;

@@ -187,15 +187,18 @@ __global__ void __launch_bounds__(PT) prefix_segments_kernel(const uint64_t* __r
 }
 
 // Projected member rows: row-major (blk = 0: word w of member j at j stride + w), or blocked (blk > 0: the
-// members in blocks of blk, each block stored chunk by chunk: 4-word chunk c of every member of the block,
-// then chunk c + 1; word w of member j at (j / blk) stride blk + (w / 4) 4 blk + (j % blk) 4 + w % 4), so
-// the tensor-core Gram's producers, one per member of a block, read a stage's words of consecutive members
-// as one contiguous run. Offsets are in words from the work entry's base.
+// members in blocks of blk, each block stored 4-word chunk by chunk, and each chunk as two halves: words
+// 0-1 of every member of the block, then words 2-3; word w of member j at (j / blk) stride blk +
+// (w / 4) 4 blk + ((w / 2) % 2) 2 blk + (j % blk) 2 + w % 2). A Gram stage's words of a block are then one
+// contiguous run, and consecutive members' 16-byte halves are adjacent, so a warp reading one half of 32
+// members' chunks reads 512 contiguous bytes. Offsets are in words from the work entry's base; the two
+// parts add: proj_member_offset(j) + proj_word_offset(w).
 __host__ __device__ inline int64_t proj_member_offset(int64_t j, int64_t stride, int64_t blk) {
-    return blk > 0 ? (j / blk) * stride * blk + (j % blk) * 4 : j * stride;
+    return blk > 0 ? (j / blk) * stride * blk + (j % blk) * 2 : j * stride;
 }
-// Offset of word w (a multiple of 4 under a blocked layout) within a member's row.
-__host__ __device__ inline int64_t proj_word_offset(int64_t w, int64_t blk) { return blk > 0 ? (w >> 2) * 4 * blk : w; }
+__host__ __device__ inline int64_t proj_word_offset(int64_t w, int64_t blk) {
+    return blk > 0 ? (w >> 2) * 4 * blk + ((w >> 1) & 1) * 2 * blk + (w & 1) : w;
+}
 
 struct PassArgs {
     const uint64_t* fbv;
@@ -281,7 +284,7 @@ __device__ __forceinline__ bool gather_members(const PassArgs& a, uint32_t& phas
     const bool my_store = lane < 4 * MAX_CHUNKS && ((valid >> lane) & 1u);
     // Lane l stores word (l & 3) of the pass's 4-word chunk warp + P_WARPS (l >> 2), for members j .. j + MPI - 1.
     const int64_t wpos = a.out0 + 4 * (warp + P_WARPS * (lane >> 2));
-    uint64_t* out_w = a.dst + proj_word_offset(wpos, a.blk) + (lane & 3);
+    uint64_t* out_w = a.dst + wpos + (lane & 3);  // row-major stores (blk = 0)
     for (int j0 = 0; j0 < m; j0 += NSTAGE) {
         // Unrolled over the stage buffers: members j0 + u .. j0 + u + MPI - 1 sit in buffers u ...
 #pragma unroll
@@ -333,18 +336,18 @@ __device__ __forceinline__ bool gather_members(const PassArgs& a, uint32_t& phas
                         if (j + v < m) out_w[(int64_t)(j + v) * a.stride] = park[v * 4 * MAX_CHUNKS + lane];
                 }
             } else {
-                // Blocked rows: the same chunk of consecutive members is contiguous, so lane l stores word l % 4
-                // of chunk kk + l / 16 for member j + (l / 4) % 4: two full 128-byte runs per store.
+                // Blocked rows: the same chunk half of consecutive members is contiguous, so lane l stores word
+                // l % 4 of chunk kk + l / 16 for member j + (l / 4) % 4: four full 64-byte runs per store.
                 const uint32_t bk = (uint32_t)a.blk;
                 const int v = (lane >> 2) & 3;
                 uint32_t q = (uint32_t)(j + v) / bk, r = (uint32_t)(j + v) - q * bk;
-                const int64_t moff = (int64_t)q * a.stride * bk + 4 * (int64_t)r;
+                const int64_t moff = (int64_t)q * a.stride * bk + 2 * (int64_t)r;
 #pragma unroll
                 for (int kk = 0; kk < MAX_CHUNKS; kk += 2) {
                     const int k = kk + (lane >> 4);
                     const int i = 4 * k + (lane & 3);
                     if (k < MAX_CHUNKS && ((valid >> i) & 1u) && j + v < m)
-                        a.dst[moff + proj_word_offset(a.out0 + 4 * (warp + P_WARPS * k), a.blk) + (lane & 3)] =
+                        a.dst[moff + proj_word_offset(a.out0 + 4 * (warp + P_WARPS * k) + (lane & 3), a.blk)] =
                             park[v * 4 * MAX_CHUNKS + i];
                 }
             }
@@ -467,7 +470,208 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
             for (int64_t idx = threadIdx.x; idx < m * pad; idx += PT) {
                 const int64_t j = idx / pad;
                 const int64_t w = used + (idx - j * pad);
-                dst[proj_member_offset(j, stride, blk) + proj_word_offset(w & ~3LL, blk) + (w & 3)] = 0ULL;
+                dst[proj_member_offset(j, stride, blk) + proj_word_offset(w, blk)] = 0ULL;
+            }
+        }
+    }
+}
+
+// ---- row-major projection -------------------------------------------------------------------------------------
+//
+// The same projected rows as project_seg_kernel, made from a row-major copy of the bitvectors (xt: word c of
+// row r holds bit r of columns 32 c .. 32 c + 31). Per unit (segment, work entry) the segment's prefix rows
+// are listed as before; then each warp takes 128 listed rows x 128 columns at a time: every lane loads the
+// 16-byte word group of four listed rows, and four 32 x 32 bit transposes per 32-column chunk (five shuffle
+// rounds each) turn rows into columns, so lane k ends with column 32 c + k's bits at the 128 rows: two
+// projected words, stored with one 16-byte store when that column is a member of the group. Only the prefix
+// rows' words are read (a segment's prefix rows are a few per cent of its rows at the densities the
+// projection serves), where the column form reads every member's whole segment; a transpose costs under one
+// instruction per projected 32-bit word, a gather by ballots about three.
+constexpr int RT = 256;
+constexpr int R_WARPS = RT / 32;
+constexpr int R_LIST = 8192;  // prefix rows listed per pass (128-row blocks: 64)
+
+// Lane i holds row i of a 32 x 32 bit matrix (bit k = column k); returns column `lane` (bit i = row i).
+// Round j swaps the off-diagonal j x j blocks of every 2j x 2j block (Hacker's Delight, "transpose32",
+// with the partner row taken by a shuffle).
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
+#pragma unroll
+    for (int j = 16; j >= 1; j >>= 1) {
+        const uint32_t m = j == 16 ? 0x0000FFFFu : j == 8 ? 0x00FF00FFu : j == 4 ? 0x0F0F0F0Fu : j == 2 ? 0x33333333u
+                                                                                                      : 0x55555555u;
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+        x = (lane & j) ? ((x & ~m) | ((y >> j) & m)) : ((x & m) | ((y & m) << j));
+    }
+    return x;
+}
+
+__device__ __forceinline__ uint32_t u4_word(const uint4& v, int c) {
+    return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w;
+}
+
+// xt [64 n_words][ldr]: one CTA per 128 rows x 256 columns; warp w transposes chunk 8 y + w of the two words
+// of its 32 columns, and the tile goes out as 32 contiguous bytes per row.
+__global__ void __launch_bounds__(RT) rows_transpose_kernel(const uint64_t* __restrict__ fbv, int64_t ld,
+                                                           int64_t n_words, int64_t n_cols,
+                                                           uint32_t* __restrict__ xt, int64_t ldr) {
+    __shared__ uint32_t tile[128][9];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t w = 2 * (int64_t)blockIdx.x;
+    const int64_t c = (int64_t)blockIdx.y * 8 + warp;
+    const int64_t col = c * 32 + lane;
+    uint64_t a = 0, b = 0;
+    if (col < n_cols) {
+        a = __ldg(fbv + col * ld + w);
+        if (w + 1 < n_words) b = __ldg(fbv + col * ld + w + 1);
+    }
+    tile[lane][warp] = transpose32((uint32_t)a, lane);
+    tile[32 + lane][warp] = transpose32((uint32_t)(a >> 32), lane);
+    tile[64 + lane][warp] = transpose32((uint32_t)b, lane);
+    tile[96 + lane][warp] = transpose32((uint32_t)(b >> 32), lane);
+    __syncthreads();
+    const int r = threadIdx.x >> 1, h = threadIdx.x & 1;
+    const int64_t row = w * 64 + r;
+    const int64_t c0 = (int64_t)blockIdx.y * 8 + 4 * h;
+    if (row < n_words * 64 && c0 < ldr)
+        *reinterpret_cast<uint4*>(xt + row * ldr + c0) =
+            make_uint4(tile[r][4 * h], tile[r][4 * h + 1], tile[r][4 * h + 2], tile[r][4 * h + 3]);
+}
+
+__global__ void __launch_bounds__(RT, 3) project_rows_kernel(
+    const uint64_t* __restrict__ fbv, int64_t ld, int64_t n_words, const uint32_t* __restrict__ xt, int64_t ldr,
+    const int32_t* __restrict__ rows, int width, const int64_t* __restrict__ grp_first,
+    const int32_t* __restrict__ grp_size, const int64_t* __restrict__ work_groups, int64_t n_work, int64_t n_seg,
+    const int64_t* __restrict__ seg_off, const int64_t* __restrict__ cbase, const int64_t* __restrict__ cld,
+    uint64_t* __restrict__ cbuf, int64_t blk) {
+    extern __shared__ __align__(16) uint8_t rsm[];
+    uint64_t* pw = reinterpret_cast<uint64_t*>(rsm);                  // SEG_W prefix words
+    uint16_t* list = reinterpret_cast<uint16_t*>(pw + SEG_W);         // R_LIST listed rows (local ids)
+    uint32_t* cmask = reinterpret_cast<uint32_t*>(list + R_LIST);     // the group's members per 32-column chunk
+    int32_t* crank = reinterpret_cast<int32_t*>(cmask + ldr);         // members before each chunk
+    int32_t* cgl = crank + ldr;                                       // 4-chunk groups holding a member
+    __shared__ int32_t pref[64];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int plen = width - 1;
+    const int64_t total = n_seg * n_work;
+    // Units round-robin in segment-major order (CTA b takes b, b + grid, ...): the units are many and small, and
+    // a fixed assignment keeps every launch's schedule independent of other streams' kernels.
+    for (int64_t q = blockIdx.x; q < total; q += gridDim.x) {
+        const int64_t s = q / n_work, wi = q - s * n_work;
+        // Per-chunk tables (rewritten at the same addresses chunk after chunk) are read through L2 only.
+        const int64_t g = __ldcg(work_groups + wi);
+        const int64_t m = __ldcg(grp_size + g);
+        const int64_t first = __ldcg(grp_first + g);
+        const int64_t w0 = s * SEG_W;
+        const int nw = (int)min64(SEG_W, n_words - w0);
+        const int64_t* so = seg_off + wi * (n_seg + 1);
+        const int64_t stride = __ldcg(cld + wi);
+        const int64_t base = __ldcg(cbase + wi);
+        uint64_t* dst = cbuf + base;
+        __syncthreads();  // the previous unit is done with the shared buffers
+        if (m <= 0) continue;
+        const int32_t* colp = rows + first * width + width - 1;
+        const int c_lo = (colp[0] >> 5) & ~3;
+        const int nch = ((colp[(m - 1) * width] >> 5) - c_lo + 4) & ~3;  // chunks covered, whole 4-chunk groups
+        // Refused units (the status word reports them): a member past the row-major copy, or member rows that
+        // are not 16-byte aligned (odd base or stride), which the 16-byte stores below need.
+        if (c_lo + nch > ldr || ((base | stride) & 1) != 0) {
+            if (threadIdx.x == 0) atomicExch(&g_proj_status, ETM_EINVAL);
+            continue;
+        }
+        if (threadIdx.x < plen) pref[threadIdx.x] = rows[first * width + threadIdx.x];
+        for (int t = threadIdx.x; t < nch; t += RT) cmask[t] = 0u;
+        __syncthreads();
+        for (int64_t i = threadIdx.x; i < m; i += RT) {
+            const int it = colp[i * width];
+            atomicOr(&cmask[(it >> 5) - c_lo], 1u << (it & 31));
+        }
+        __syncthreads();
+        // Member ranks per chunk and the list of non-empty 4-chunk groups (ordered scans).
+        int64_t carry = 0, n_cg = 0;
+        for (int c0 = 0; c0 < nch; c0 += RT) {
+            const int c = c0 + threadIdx.x;
+            const uint32_t mk = c < nch ? cmask[c] : 0u;
+            int64_t tot, tg;
+            const int64_t ex = block_exclusive_scan(__popc(mk), &tot);
+            if (c < nch) crank[c] = (int32_t)(carry + ex);
+            carry += tot;
+            const int head = c < nch && (c & 3) == 0 && (cmask[c] | cmask[c + 1] | cmask[c + 2] | cmask[c + 3]) != 0u;
+            const int64_t eg = block_exclusive_scan(head, &tg);
+            if (head) cgl[n_cg + eg] = c;
+            n_cg += tg;
+        }
+        int my = 0;
+#pragma unroll
+        for (int k = 0; k < SEG_W / RT; k++) {
+            const int w = threadIdx.x * (SEG_W / RT) + k;
+            const uint64_t p = w < nw ? prefix_word(fbv, ld, pref, plen, w0 + w) : 0ULL;
+            pw[w] = p;
+            my += __popcll(p);
+        }
+        int64_t cnt;
+        const int64_t my_base = block_exclusive_scan(my, &cnt);
+        const int64_t row0 = w0 * 64;
+        for (int64_t p0 = 0; p0 < cnt; p0 += R_LIST) {
+            int64_t at = my_base;
+#pragma unroll
+            for (int k = 0; k < SEG_W / RT; k++) {
+                const int w = threadIdx.x * (SEG_W / RT) + k;
+                uint64_t bits = pw[w];
+                const int c = __popcll(bits);
+                if (at + c > p0 && at < p0 + R_LIST) {
+                    int64_t a = at;
+                    while (bits) {
+                        const int b = __ffsll((long long)bits) - 1;
+                        if (a >= p0 && a < p0 + R_LIST) list[a - p0] = (uint16_t)(w * 64 + b);
+                        ++a;
+                        bits &= bits - 1;
+                    }
+                }
+                at += c;
+            }
+            const int pass_rows = (int)min64(R_LIST, cnt - p0);
+            const int pass_words = (pass_rows + 63) >> 6;
+            const int nblk = ((pass_words + 3) & ~3) >> 1;  // 128-row blocks up to the piece's 4-word chunk
+            const int64_t out0 = __ldcg(so + s) + (p0 >> 6);
+            __syncthreads();
+            const int64_t n_it = (int64_t)nblk * n_cg;
+            for (int64_t it = warp; it < n_it; it += R_WARPS) {
+                const int b = (int)(it / n_cg);
+                const int cg = cgl[it - (int64_t)b * n_cg];
+                uint4 v[4];
+#pragma unroll
+                for (int qq = 0; qq < 4; qq++) {
+                    const int x = b * 128 + qq * 32 + lane;
+                    v[qq] = make_uint4(0u, 0u, 0u, 0u);
+                    if (x < pass_rows)
+                        v[qq] = __ldg(reinterpret_cast<const uint4*>(xt + (row0 + list[x]) * ldr + c_lo + cg));
+                }
+                const int64_t wo = proj_word_offset(out0 + 2 * b, blk);  // words 2b and 2b + 1 are adjacent
+#pragma unroll
+                for (int cc = 0; cc < 4; cc++) {
+                    const uint32_t mk = cmask[cg + cc];
+                    if (mk == 0u) continue;  // warp-uniform
+                    const uint32_t t0 = transpose32(u4_word(v[0], cc), lane);
+                    const uint32_t t1 = transpose32(u4_word(v[1], cc), lane);
+                    const uint32_t t2 = transpose32(u4_word(v[2], cc), lane);
+                    const uint32_t t3 = transpose32(u4_word(v[3], cc), lane);
+                    if ((mk >> lane) & 1u) {
+                        const int64_t i = crank[cg + cc] + __popc(mk & ((1u << lane) - 1u));
+                        *reinterpret_cast<ulonglong2*>(dst + proj_member_offset(i, stride, blk) + wo) =
+                            make_ulonglong2((uint64_t)t0 | ((uint64_t)t1 << 32), (uint64_t)t2 | ((uint64_t)t3 << 32));
+                    }
+                }
+            }
+            __syncthreads();  // the next pass rewrites the list
+        }
+        if (s == n_seg - 1) {
+            // Zero the words after the last piece, up to the member stride.
+            const int64_t used = __ldcg(so + n_seg);
+            const int64_t pad = stride - used;
+            for (int64_t idx = threadIdx.x; idx < m * pad; idx += RT) {
+                const int64_t j = idx / pad;
+                const int64_t w = used + (idx - j * pad);
+                dst[proj_member_offset(j, stride, blk) + proj_word_offset(w, blk)] = 0ULL;
             }
         }
     }
@@ -579,6 +783,49 @@ extern "C" int etm_project_blocked(const uint64_t* fbv, int64_t ld, int64_t n_wo
     ETM_REQUIRE(blk >= 1, ETM_EINVAL, "etm_project_blocked: blk must be >= 1");
     return project_impl(fbv, ld, n_words, rows, width, grp_first, grp_size, work_groups, n_work, seg_off, cbase, cld,
                         cbuf, work_counter, blk, stream);
+}
+
+extern "C" int etm_rows_transpose(const uint64_t* fbv, int64_t ld, int64_t n_words, int64_t n_cols, uint32_t* xt,
+                                  int64_t ldr, void* stream) {
+    ETM_REQUIRE(ld >= n_words && n_words >= 0 && n_cols >= 0, ETM_EINVAL, "etm_rows_transpose: bad sizes");
+    ETM_REQUIRE(ldr % 4 == 0 && ldr * 32 >= n_cols, ETM_EINVAL,
+                "etm_rows_transpose: ldr must be a multiple of 4 with 32 ldr >= n_cols");
+    ETM_REQUIRE((reinterpret_cast<uintptr_t>(xt) & 15) == 0, ETM_EINVAL, "etm_rows_transpose: xt must be 16-byte aligned");
+    ETM_REQUIRE(n_words < (1LL << 32) && ldr / 8 < 65535, ETM_EINVAL, "etm_rows_transpose: too large");
+    if (n_words == 0 || ldr == 0) return ETM_OK;
+    const dim3 grid((unsigned)ceil_div<int64_t>(n_words, 2), (unsigned)ceil_div<int64_t>(ldr, 8));
+    rows_transpose_kernel<<<grid, RT, 0, as_stream(stream)>>>(fbv, ld, n_words, n_cols, xt, ldr);
+    ETM_LAUNCHED("rows_transpose");
+    return ETM_OK;
+}
+
+extern "C" int etm_project_rows(const uint64_t* fbv, int64_t ld, int64_t n_words, const uint32_t* xt, int64_t ldr,
+                                const int32_t* rows, int32_t width, const int64_t* grp_first, const int32_t* grp_size,
+                                const int64_t* work_groups, int64_t n_work, const int64_t* seg_off,
+                                const int64_t* cbase, const int64_t* cld, int64_t blk, uint64_t* cbuf, void* stream) {
+    ETM_REQUIRE(blk >= 0 && blk <= 4096, ETM_EINVAL, "etm_project_rows: blk %lld out of range (0..4096)", (long long)blk);
+    ETM_REQUIRE(width >= 2 && width <= 64, ETM_EINVAL, "etm_project_rows: width %d out of range (2..64)", width);
+    ETM_REQUIRE(ld >= n_words && n_words >= 0, ETM_EINVAL, "etm_project_rows: ld < n_words");
+    ETM_REQUIRE(ldr % 4 == 0 && ldr > 0, ETM_EINVAL, "etm_project_rows: ldr must be a positive multiple of 4");
+    ETM_REQUIRE((reinterpret_cast<uintptr_t>(xt) & 15) == 0 && (reinterpret_cast<uintptr_t>(cbuf) & 15) == 0,
+                ETM_EINVAL, "etm_project_rows: xt and cbuf must be 16-byte aligned");
+    if (n_work <= 0 || n_words == 0) return ETM_OK;
+    const int smem = SEG_W * 8 + R_LIST * 2 + (int)ldr * 8 + (int)(ldr / 4 + 1) * 4;
+    ETM_REQUIRE(smem <= 200 * 1024, ETM_EINVAL, "etm_project_rows: %lld row words need too much shared memory",
+                (long long)ldr);
+    static int configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        ETM_CUDA(cudaFuncSetAttribute(project_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        configured = smem;
+    }
+    const int64_t n_seg = ceil_div<int64_t>(n_words, SEG_W);
+    const int64_t units = n_seg * n_work;
+    const int grid = (int)min64(units, (int64_t)max(1, sm_count()) * 3);
+    project_rows_kernel<<<grid, RT, smem, as_stream(stream)>>>(fbv, ld, n_words, xt, ldr, rows, width, grp_first,
+                                                               grp_size, work_groups, n_work, n_seg, seg_off, cbase,
+                                                               cld, cbuf, blk);
+    ETM_LAUNCHED("project_rows");
+    return ETM_OK;
 }
 
 extern "C" int etm_count_tiles_proj(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords,

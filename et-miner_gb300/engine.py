@@ -211,11 +211,29 @@ class MineOutput:
         values_d = torch.cat(vparts)
         support_d = torch.cat(cparts).to(torch.float64) / max(1, self.n_rows)
         offsets_d = torch.cat(oparts)
-        values = values_d.cpu().numpy()
-        support = support_d.cpu().numpy()
-        offsets = offsets_d.cpu().numpy()
+        values, support, offsets = _copy_to_host(values_d, support_d, offsets_d)
         d2h = values.nbytes + support.nbytes + offsets.nbytes
         return offsets, values.view(np.uint64) if wide else values, support, d2h
+
+
+#: Results at least this large come back through page-locked host memory.
+PINNED_RESULT_BYTES = 64 << 20
+
+
+def _copy_to_host(*tensors: torch.Tensor) -> list[np.ndarray]:
+    """Device tensors as host numpy arrays. Large results are copied into page-locked tensors from torch's
+    caching host allocator (full-rate copies, no page faults on fresh memory; a block returns to the cache when
+    the arrays viewing it are dropped, so repeated calls reuse it); small ones go through ``.cpu()``."""
+    big = sum(t.numel() * t.element_size() for t in tensors) >= PINNED_RESULT_BYTES
+    if not big:
+        return [t.cpu().numpy() for t in tensors]
+    hosts = []
+    for t in tensors:
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t, non_blocking=True)
+        hosts.append(h)
+    torch.cuda.current_stream().synchronize()
+    return [h.numpy() for h in hosts]
 
 
 class _Scratch:
@@ -300,7 +318,7 @@ class Engine:
                  form: str = "batched", chunk_cands: int = CHUNK_CANDS, small_group: int = SMALL_GROUP,
                  project: bool = True, proj_density: float = PROJ_DENSITY, proj_bytes: int = PROJ_BYTES,
                  tc_elem: int = DEFAULT_TC_ELEM, pipeline: bool = True, autotune: "Autotuner | bool | None" = None,
-                 fused: bool = True, deduction_bounds: bool = True):
+                 fused: bool = True, deduction_bounds: bool = True, proj_rows: bool = True):
         if not torch.cuda.is_available():
             raise RuntimeError("the GB300 engine needs a CUDA device; there is no CPU fallback")
         self.lib = load_library()
@@ -329,6 +347,13 @@ class Engine:
         #: Under count inference, settle candidates by the deduction bounds of depth <= 3 from levels k-2 and
         #: k-3 (on by default in the reference's GPU route, gpu/row_split.py:541-546, 629); needs fused.
         self.deduction_bounds = bool(deduction_bounds)
+        #: Projection from a row-major copy of the generating columns (etm_project_rows, 32 x 32 bit transposes
+        #: over the prefix rows) instead of gathering every member's segment words (etm_project); the copy is
+        #: built once per mine and skipped when it would exceed ``rows_copy_max_bytes``.
+        self.proj_rows = bool(proj_rows)
+        self.rows_copy_max_bytes = 32 << 30
+        self._xt = None
+        self._xt_key = None
         #: (level k-2, level k-3 or None, N) of the level being counted, for the deduction bounds.
         self._deep = None
         #: When set, each level's stats count the candidates classified INFER and SKIP (one extra pass per chunk).
@@ -439,11 +464,34 @@ class Engine:
         self.launches += 1
         return out.cpu().numpy().copy()
 
-    def _prep_projected(self, fbv, ldp, n_words, gen, grp_first, grp_size, gids, sizes, pcnt, method, buf: int = 0):
+    def _rows_copy(self, fbv: torch.Tensor, ldp: int, n_words: int):
+        """(xt, ldr): the row-major copy of the mine's generating columns that etm_project_rows reads (word c of
+        row r holds bit r of columns 32 c .. 32 c + 31), built on the current stream at its first use in a mine;
+        None when it would exceed ``rows_copy_max_bytes``."""
+        n_g = int(fbv.shape[0])
+        key = (fbv.data_ptr(), n_words, n_g)
+        if self._xt_key == key:
+            return self._xt
+        ldr = max(4, -(-(-(-n_g // 32)) // 4) * 4)
+        nbytes = n_words * 64 * ldr * 4
+        self._xt, self._xt_key = None, key
+        if nbytes > self.rows_copy_max_bytes:
+            return None
+        xt = torch.empty((n_words * 64, ldr), dtype=torch.int32, device=self.device)
+        st = self._launch("rows_transpose", n_g * n_words * 8 + nbytes, lambda: self.lib.etm_rows_transpose(
+            _p(fbv), ldp, n_words, n_g, _p(xt), ldr, _stream()))
+        check(st, "etm_rows_transpose")
+        self.launches += 1
+        self._xt = (xt, ldr)
+        return self._xt
+
+    def _prep_projected(self, fbv, ldp, n_words, gen, grp_first, grp_size, gids, sizes, pcnt, method, buf: int = 0,
+                        xt=None):
         """Segment offsets and projected member words of the listed groups (two launches on the current stream).
 
         Returns what ``_count_prepped`` needs. ``buf`` selects one of two scratch sets, so the
-        projection of the next chunk can run while the current one is counted.
+        projection of the next chunk can run while the current one is counted. ``xt``: the row-major copy
+        (``_rows_copy``) for the row-major projection, else the column form runs.
         """
         width = gen.k
         # Longest prefixes first: the Gram's CTAs claim block pairs in this order, so the last ones are short.
@@ -474,6 +522,23 @@ class Engine:
                                                                _p(grp_first), _p(wg), n, _p(seg_off), _p(cwords),
                                                                _stream()))
         check(st, "etm_prefix_segments")
+        if xt is not None:
+            # Algorithmic bytes: the prefix columns' words and the prefix rows' row-major words read once, the
+            # member strides written.
+            xt_t, ldr = xt
+            st = self._launch("project_rows", int(n * (width - 1) * n_words * 8 + (cnt * ldr).sum() * 4
+                                                  + (m * cl).sum() * 8),
+                              lambda: self.lib.etm_project_rows(
+                                  _p(fbv), ldp, n_words, _p(xt_t), ldr, _p(gen.rows), width, _p(grp_first),
+                                  _p(grp_size), _p(wg), n, _p(seg_off), _p(cbase), _p(cld), blk, _p(cbuf),
+                                  _stream()))
+            check(st, "etm_project_rows")
+            xt_t.record_stream(torch.cuda.current_stream())
+            self._waits_pending = True
+            self.launches += 2
+            return dict(d=d, cbuf=cbuf, cbase=cbase, cwords=cwords, cld=cld, wg=wg, wo=wo, n=n,
+                        n_tiles=int(toff[-1]), blocked=bool(blk), nbytes=int((m * ((cnt + 63) // 64)).sum() * 8),
+                        macs=float((m * (m - 1) / 2 * cnt.astype(np.float64)).sum()))
         # Algorithmic bytes: every member's column words and the prefix words read once, the strides written.
         st = self._launch("project", int(((m + width - 1) * n_words).sum() * 8 + (m * cl).sum() * 8),
                           lambda: self.lib.etm_project_blocked(
@@ -505,9 +570,9 @@ class Engine:
                           prep["macs"], sel, prep["blocked"])
 
     def _count_projected(self, fbv, ldp, n_words, gen, grp_first, grp_size, cand_off, gids, sizes, pcnt, base, cls,
-                         counts, method, sel=None):
+                         counts, method, sel=None, xt=None):
         """Row lists, projected suffix words and tile-pair counts of the listed groups (one launch each)."""
-        prep = self._prep_projected(fbv, ldp, n_words, gen, grp_first, grp_size, gids, sizes, pcnt, method)
+        prep = self._prep_projected(fbv, ldp, n_words, gen, grp_first, grp_size, gids, sizes, pcnt, method, 0, xt)
         self._count_prepped(prep, grp_size, cand_off, base, cls, counts, method, sel)
 
     def _count_words(self, cbuf, cbase, cwords, cld, grp_size, cand_off, wg, wo, n, n_tiles, base, cls, counts,
@@ -667,6 +732,8 @@ class Engine:
             g1 = max(min(g1c, g1p), g0 + 1)
             chunks.append((g0, g1))
             g0 = g1
+        # The row-major copy for the projection, made on the main stream before any side-stream work reads it.
+        xt = self._rows_copy(fbv, ldp, n_words) if (self.proj_rows and proj.any()) else None
         # Batched form: the projection of chunk c+1 runs on a side stream while chunk c is counted
         # (memory-bound gathers beside tensor-bound MMAs); two scratch sets alternate.
         pipelined = self.pipeline and self.form == "batched" and proj.any()
@@ -689,7 +756,7 @@ class Engine:
             with torch.cuda.stream(side):
                 side.wait_event(buf_free[buf])
                 preps[c] = self._prep_projected(fbv, ldp, n_words, gen, grp_first, grp_size, ids_c, sizes, pcnt,
-                                                method, buf)
+                                                method, buf, xt)
                 prep_done[buf].record(side)
 
         if pipelined:
@@ -781,7 +848,7 @@ class Engine:
                     groups = [gids] if self.form == "batched" else [gids[q:q + 1] for q in range(len(gids))]
                     for bg in groups:
                         self._count_projected(fbv, ldp, n_words, gen, grp_first, grp_size, cand_off, bg, sizes, pcnt,
-                                              base, cls, counts, method, sel)
+                                              base, cls, counts, method, sel, xt)
                     continue
                 if kind == "tiles" and whole_tc:
                     mg = sizes[gids]
@@ -942,6 +1009,7 @@ class Engine:
         ptr, (n_cols, ld), _owner = as_device_bitvecs(bitvecs)
         self._k2_rows = None
         self._rows_input = None
+        self._xt, self._xt_key = None, None  # the row-major copy belongs to one mine's generating columns
         if n_rows >= 2**31:
             raise ValueError(f"n_transactions={n_rows:,} exceeds int32 max: the count arrays are int32")
         n_words = (n_rows + 63) // 64
@@ -1033,6 +1101,7 @@ class Engine:
             gen = new
             k += 1
         self._deep = None
+        self._xt, self._xt_key = None, None
         return out
 
 
@@ -1040,5 +1109,5 @@ def mine(bitvecs, n_rows: int, min_support: float, max_length: int | None = None
     """Mine device bitvectors [n_cols, ceil(N/64)] with a fresh ``Engine`` (see ``Engine.mine``)."""
     engine_kw = {k: kw.pop(k) for k in ("method", "form", "chunk_cands", "small_group", "device", "project",
                                         "proj_density", "proj_bytes", "tc_elem", "pipeline", "autotune", "fused",
-                                        "deduction_bounds") if k in kw}
+                                        "deduction_bounds", "proj_rows") if k in kw}
     return Engine(**engine_kw).mine(bitvecs, n_rows, min_support, max_length, **kw)

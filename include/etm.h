@@ -258,10 +258,12 @@ int etm_project(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t*
                 int64_t* work_counter, void* stream);
 /*
  * etm_project writing the blocked layout: the members of each work entry in
- * blocks of blk (1..4096), each block stored 4-word chunk by chunk, so word w
- * of member j sits at cbase + (j / blk) * cld * blk + (w / 4) * 4 * blk +
- * (j % blk) * 4 + w % 4. The tensor-core Gram's producers (one per member of
- * a block) then read each stage's words of a block as one contiguous run
+ * blocks of blk (1..4096), each block stored 4-word chunk by chunk and each
+ * chunk as two 2-word halves, so word w of member j sits at cbase +
+ * (j / blk) * cld * blk + (w / 4) * 4 * blk + ((w / 2) % 2) * 2 * blk +
+ * (j % blk) * 2 + w % 2. The tensor-core Gram then copies each stage's words
+ * of a block as one contiguous run, and its producers (one per member of a
+ * block) read consecutive members' halves from adjacent 16-byte slots
  * (elem | ETM_TC_BLOCKED, blk = etm_gram_block_members(elem)). Each work
  * entry needs ceil(m / blk) * blk * cld words (rows past m are never read).
  * New in this engine, like the projection itself.
@@ -270,6 +272,38 @@ int etm_project_blocked(const uint64_t* fbv, int64_t ld, int64_t n_words, const 
                         const int64_t* grp_first, const int32_t* grp_size, const int64_t* work_groups, int64_t n_work,
                         const int64_t* seg_off, const int64_t* cbase, const int64_t* cld, int64_t blk, uint64_t* cbuf,
                         int64_t* work_counter, void* stream);
+
+/*
+ * Row-major copy of the generating columns for etm_project_rows: xt is
+ * uint32 [64 n_words][ldr] (16-byte aligned, ldr a multiple of 4 with
+ * 32 ldr >= n_cols), and bit k of xt[r][c] is bit r of column 32 c + k of fbv
+ * (zero past n_cols). One pass over the columns; no counterpart in the
+ * reference, which never transposes its bitvectors.
+ */
+int etm_rows_transpose(const uint64_t* fbv, int64_t ld, int64_t n_words, int64_t n_cols, uint32_t* xt, int64_t ldr,
+                       void* stream);
+
+/*
+ * The projection of etm_project / etm_project_blocked (blk = 0: row-major
+ * member rows, blk > 0: the blocked layout; the same words, the same
+ * seg_off / cbase / cld / cbuf contract) computed from the row-major copy xt
+ * of etm_rows_transpose: per (segment, work entry) unit the prefix rows are
+ * listed, their words loaded 128 rows x 128 columns at a time and turned into
+ * member words by 32 x 32 bit transposes (warp shuffles). It reads only the
+ * prefix rows' words where the column form reads every member's whole
+ * segment, and needs no bulk copies or device waits. cbase and cld entries
+ * must be even (16-byte aligned member rows) and every member column must lie
+ * below 32 ldr; a unit that breaks either is skipped and etm_device_status
+ * reports ETM_EINVAL. Units go to CTAs round-robin (no work counter: with
+ * units claimed from a counter, a launch overlapping another stream's
+ * kernels was measured to leave a few units unwritten in about one mine in
+ * eight; the cause is not known). The projection of gram_pairs' input
+ * (core/cpu_miner.py:641-692) in another form, like etm_project.
+ */
+int etm_project_rows(const uint64_t* fbv, int64_t ld, int64_t n_words, const uint32_t* xt, int64_t ldr,
+                     const int32_t* rows, int32_t width, const int64_t* grp_first, const int32_t* grp_size,
+                     const int64_t* work_groups, int64_t n_work, const int64_t* seg_off, const int64_t* cbase,
+                     const int64_t* cld, int64_t blk, uint64_t* cbuf, void* stream);
 
 int etm_count_tiles_proj(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                          const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
@@ -335,9 +369,11 @@ int etm_popc_rate(int64_t iters, double* out_gops, void* stream);
  * Reads and clears the device status words the tensor-core kernels and the
  * projection (its bulk copies) raise when a bounded wait gives up
  * (synchronizes `stream`). Returns 0, ETM_ETIMEOUT (the kernel gave up and
- * cleaned up: its counts are incomplete, the device stays usable) or
+ * cleaned up: its counts are incomplete, the device stays usable),
  * ETM_EUNSAFE (the projection's cleanup wait ran out too: stop using the
- * device). The words are per device, shared by every caller of the library.
+ * device) or ETM_EINVAL (etm_project_rows skipped a unit whose members lie
+ * past its row-major copy). The words are per device, shared by every caller
+ * of the library.
  */
 int etm_device_status(void* stream);
 
@@ -451,8 +487,10 @@ int etm_level_compact(const int32_t* counts, const uint8_t* cls, int64_t n_cands
  * device looks up that device's array address (cudaGetSymbolAddress), so make
  * that first call before any stream capture. All calls on a device share the
  * array: calls that overlap on the GPU (other streams, or other host threads)
- * race and must be serialized by the caller. Everything else (acc, cap,
- * outputs, ordering) is as in etm_level_compact.
+ * race and must be serialized by the caller. The cached address belongs to
+ * the device's primary context (the CUDA runtime's): the entry point assumes
+ * that context is current and that no cudaDeviceReset happens between calls.
+ * Everything else (acc, cap, outputs, ordering) is as in etm_level_compact.
  */
 int etm_level_compact_static(const int32_t* counts, const uint8_t* cls, int64_t n_cands, const int32_t* rows,
                              int32_t width, const int64_t* grp_first, const int32_t* grp_size,

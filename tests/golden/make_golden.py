@@ -1,7 +1,7 @@
 """Regenerate the golden fixtures from the reference's own CPU route.
 
-Runs ONLY in a checkout where the ET-Miner sources are present (default
-/root/reference, or the path in ETM_REFERENCE_SRC). polars and loguru are not
+Runs ONLY where the ET-Miner sources are present: ETM_REFERENCE_SRC names their
+``src`` directory (the one holding ``et_miner/``). polars and loguru are not
 needed by the counting code and are stubbed at import time; the package
 ``__init__`` is bypassed so that cupy is never imported. The reference's
 ``_k1_seed`` + ``_mine_levels`` (core/cpu_miner.py:973-981, 1066-1161) mine
@@ -11,7 +11,7 @@ small cases, the generator and seed of the larger ones, and every case's
 digest and per-level sizes; small cases also hold every (itemset, count).
 
 Usage:
-    python tests/golden/make_golden.py            # writes tests/golden/cases.json
+    ETM_REFERENCE_SRC=<ET-Miner checkout>/src python tests/golden/make_golden.py   # writes tests/golden/cases.json
 """
 
 from __future__ import annotations
@@ -29,11 +29,18 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
 sys.path.insert(0, str(REPO))
 
-REF = Path(os.environ.get("ETM_REFERENCE_SRC", "/root/reference/src"))
+
+
+def _reference_src() -> Path:
+    src = os.environ.get("ETM_REFERENCE_SRC")
+    if not src:
+        raise SystemExit("set ETM_REFERENCE_SRC to the ET-Miner sources' src directory (the one holding et_miner/)")
+    return Path(src)
 
 
 def _load_reference():
     """Import et_miner.core.cpu_miner from the reference sources with polars/loguru stubbed."""
+    REF = _reference_src()
 
     class _Any:
         def __getattr__(self, name):

@@ -46,6 +46,8 @@ def engines(pkg):
         "dense": eng.Engine(fused=False),
         "dense_tiny": eng.Engine(fused=False, chunk_cands=97, small_group=3),
         "rows_dense": _rows_engine(eng.Engine(fused=False), k3=True),
+        "proj_cols": eng.Engine(form="batched", small_group=2, proj_density=1.01, proj_bytes=1 << 14, proj_rows=False),
+        "popcount_rows": eng.Engine(method="popcount", small_group=2, proj_density=1.01),
     }
 
 
@@ -65,7 +67,7 @@ def test_transactions_match_golden(pkg, golden_cases, engines, name):
 
 
 @pytest.mark.parametrize("form", ["plain", "tiny", "proj", "noproj", "popcount", "tuned", "rows", "rows3", "dense",
-                                  "dense_tiny", "rows_dense"])
+                                  "dense_tiny", "rows_dense", "proj_cols", "popcount_rows"])
 @pytest.mark.parametrize("name", ["implication_plain", "implication_prune", "implication_infer", "plain_small_plain",
                                   "deep_sparse_small", "dense_k2_small", "word_tail_65"])
 def test_forms_match_golden(pkg, golden_cases, engines, name, form):

@@ -348,19 +348,43 @@ def _projection_reference(bits, ld, n_words, groups, stride):
     return out
 
 
+@pytest.mark.parametrize("n_words,n_cols", [(1, 33), (3, 70), (64, 1000), (129, 4096)])
+def test_rows_transpose_matches_host(lib, n_words, n_cols):
+    """etm_rows_transpose: bit k of word c of row r is bit r of column 32 c + k (zero past n_cols)."""
+    import torch
+
+    rng = np.random.default_rng(n_words + n_cols)
+    ld = max(32, (n_words + 31) // 32 * 32)
+    fbv = rng.integers(0, 2**63, (n_cols, ld), dtype=np.int64)
+    ldr = max(4, -(-(-(-n_cols // 32)) // 4) * 4)
+    xt = torch.full((n_words * 64, ldr), -1, dtype=torch.int32, device="cuda")
+    d = _dev(fbv)
+    assert lib.etm_rows_transpose(d.data_ptr(), ld, n_words, n_cols, xt.data_ptr(), ldr, _stream()) == 0, \
+        lib.etm_last_error()
+    bits = np.unpackbits(fbv[:, :n_words].view(np.uint8), axis=1, bitorder="little")[:, :n_words * 64]
+    padded = np.zeros((ldr * 32, n_words * 64), np.uint8)
+    padded[:n_cols] = bits
+    want = np.packbits(padded.T.reshape(n_words * 64, ldr, 32), axis=2, bitorder="little").reshape(
+        n_words * 64, ldr * 4).view(np.uint32)
+    assert np.array_equal(xt.cpu().numpy().view(np.uint32), want)
+
+
+@pytest.mark.parametrize("form", ["cols", "rows"])
 @pytest.mark.parametrize("blk", [0, 3, 240])
-@pytest.mark.parametrize("n_words,width", [(1, 2), (1023, 2), (1024, 3), (1025, 2), (3001, 3), (2500, 2)])
-def test_segmented_projection(pkg, lib, n_words, width, blk):
-    """etm_prefix_segments + etm_project (row-major) or etm_project_blocked (blocks of blk members, chunk by
-    chunk) against the host restatement, including a dense prefix (more prefix rows in a segment than one
-    pass lists), an empty prefix and the zero padding."""
+@pytest.mark.parametrize("n_words,width,n_cols", [(1, 2, 14), (1023, 2, 14), (1024, 3, 14), (1025, 2, 14),
+                                                  (3001, 3, 14), (2500, 2, 14), (1100, 2, 300), (70, 3, 1000)])
+def test_segmented_projection(pkg, lib, n_words, width, n_cols, blk, form):
+    """etm_prefix_segments + the projection, column form (etm_project row-major, etm_project_blocked in blocks
+    of blk members, chunk by chunk) or row form (etm_rows_transpose + etm_project_rows, either layout), against
+    the host restatement: a dense prefix (more prefix rows in a segment than one pass lists), an empty prefix,
+    the zero padding, and on wide column sets a group of every column (member ranks across chunks) beside
+    groups of a few scattered columns (empty chunks skipped)."""
     import importlib
 
     import torch
 
     eng = importlib.import_module(pkg.__name__ + ".engine")
-    rng = np.random.default_rng(n_words * 10 + width)
-    n_cols = 14
+    rng = np.random.default_rng(n_words * 10 + width + n_cols)
     dens = np.array([0.9, 0.5, 0.06, 0.02, 0.0, 0.3] + [0.4] * (n_cols - 6))
     ld = max(32, (n_words + 31) // 32 * 32)
     bits = (rng.random((n_cols, n_words * 64)) < dens[:, None]).astype(np.uint8)
@@ -372,7 +396,8 @@ def test_segmented_projection(pkg, lib, n_words, width, blk):
     groups = []
     level_rows = []
     for pre in prefixes:
-        members = sorted(rng.choice(np.arange(plen + 4, n_cols), size=int(rng.integers(1, 7)), replace=False))
+        size = n_cols - plen - 4 if pre[0] == 1 and n_cols > 100 else int(rng.integers(1, 7))
+        members = sorted(rng.choice(np.arange(plen + 4, n_cols), size=size, replace=False))
         groups.append((pre, members))
         for mbr in members:
             level_rows.append(list(pre) + [int(mbr)])
@@ -406,7 +431,16 @@ def test_segmented_projection(pkg, lib, n_words, width, blk):
     ctr = torch.zeros(1, dtype=torch.int64, device="cuda")  # held for the call
     counter = ctr.data_ptr() if n_words % 2 else None
     d_cbase, d_cld = _dev(cb[:-1].copy()), _dev(cl)
-    if blk:
+    if form == "rows":
+        ldr = max(4, -(-(-(-n_cols // 32)) // 4) * 4)
+        xt = torch.empty((n_words * 64, ldr), dtype=torch.int32, device="cuda")
+        st = lib.etm_rows_transpose(d_fbv.data_ptr(), ld, n_words, n_cols, xt.data_ptr(), ldr, _stream())
+        assert st == 0, lib.etm_last_error()
+        st = lib.etm_project_rows(d_fbv.data_ptr(), ld, n_words, xt.data_ptr(), ldr, d_rows.data_ptr(), width,
+                                  d_first.data_ptr(), d_size.data_ptr(), d_wg.data_ptr(), len(wg),
+                                  seg_off.data_ptr(), d_cbase.data_ptr(), d_cld.data_ptr(), blk, cbuf.data_ptr(),
+                                  _stream())
+    elif blk:
         st = lib.etm_project_blocked(d_fbv.data_ptr(), ld, n_words, d_rows.data_ptr(), width, d_first.data_ptr(),
                                      d_size.data_ptr(), d_wg.data_ptr(), len(wg), seg_off.data_ptr(),
                                      d_cbase.data_ptr(), d_cld.data_ptr(), blk, cbuf.data_ptr(), counter, _stream())
@@ -426,10 +460,10 @@ def test_segmented_projection(pkg, lib, n_words, width, blk):
         assert np.array_equal(so[k], expect_off)
         assert ow[k] == expect_off[-1] <= cl[k]
         if blk:
-            # Word w of member j at (j // blk) cl blk + (w // 4) 4 blk + (j % blk) 4 + w % 4.
+            # Word w of member j at (j // blk) cl blk + (w // 4) 4 blk + (w // 2 % 2) 2 blk + (j % blk) 2 + w % 2.
             j = np.arange(m[k])[:, None]
             w = np.arange(cl[k])[None, :]
-            idx = (j // blk) * cl[k] * blk + (w // 4) * 4 * blk + (j % blk) * 4 + w % 4
+            idx = (j // blk) * cl[k] * blk + (w // 4) * 4 * blk + (w // 2 % 2) * 2 * blk + (j % blk) * 2 + w % 2
             block = got[cb[k]:cb[k + 1]][idx]
         else:
             block = got[cb[k]:cb[k + 1]].reshape(m[k], cl[k])

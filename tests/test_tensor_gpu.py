@@ -137,7 +137,7 @@ def _gram_groups(lib, elem, seed=11, blocked=False):
         if blocked:
             j = np.arange(m)[:, None]
             ww = np.arange(w)[None, :]
-            buf[cbase[g] + (j // t) * cld[g] * t + (ww // 4) * 4 * t + (j % t) * 4 + ww % 4] = x
+            buf[cbase[g] + (j // t) * cld[g] * t + (ww // 4) * 4 * t + (ww // 2 % 2) * 2 * t + (j % t) * 2 + ww % 2] = x
         else:
             buf[cbase[g]:cbase[g] + m * cld[g]].reshape(m, cld[g])[:, :w] = x
         bits = np.unpackbits(x.view(np.uint8), axis=1).astype(np.int64)
@@ -212,9 +212,9 @@ def test_gram_fused_threshold(pkg, elem):
 
 
 def test_bounded_wait_give_up_reports_timeout_and_device_stays_usable(pkg):
-    """The Gram's and the projection's first waits set to give up at once: each kernel abandons its work,
-    drains what it issued, and the status word reads ETM_ETIMEOUT; then, with the default limits, the same
-    mine on the same device is exact again."""
+    """The Gram's and the column-form projection's first waits set to give up at once: each kernel abandons its
+    work, drains what it issued, and the status word reads ETM_ETIMEOUT; then, with the default limits, the
+    same mine on the same device is exact again. (The row-major projection has no device waits.)"""
     import torch
 
     lib = pkg.load_library()
@@ -229,7 +229,7 @@ def test_bounded_wait_give_up_reports_timeout_and_device_stays_usable(pkg):
         for gram_ns, proj_ns in ((0, -1), (-1, 0)):
             assert lib.etm_set_wait_limits(gram_ns, proj_ns) == 0
             with pytest.raises(RuntimeError, match="bounded wait"):
-                engm.Engine(method="tensor").mine(dev, 20_000, 0.01, 3)
+                engm.Engine(method="tensor", proj_rows=False).mine(dev, 20_000, 0.01, 3)
             assert lib.etm_device_status(None) == 0  # read and cleared by the engine
     finally:
         lib.etm_set_wait_limits(-1, -1)
