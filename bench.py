@@ -57,15 +57,15 @@ WORKLOADS = {
 
 
 #: DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic byte of a kernel, from one ncu
-#: capture of every Gram and projection launch of the 1M x 2048 dense K=2 workload (four mines: warm-up,
-#: timed step, two end-to-end calls):
+#: capture of every Gram, projection and transpose launch of the 1M x 2048 dense K=2 workload (four mines:
+#: warm-up, timed step, two end-to-end calls):
 #:   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none
-#:       -k "regex:gram_kernel|project_seg" python bench.py --workload dense_k2_mid --steps 1 --warmup 1
-#:       --no-plain --no-cpu --no-side --no-serial --no-hbm --no-pipeline
-#: per mine 15.91 GB against 12.66 GB for the Gram, 14.62 GB against 170.84 GB for the projection (its column
-#: re-reads stay in L2); the roofline's ``traffic`` scales it to the bench's own launches by their
-#: algorithmic bytes.
-DRAM_PER_ALGORITHMIC_BYTE = {"gram_tc": 15.906 / 12.659, "project": 14.624 / 170.836}
+#:       -k "regex:gram_kernel|project_rows|rows_transpose" python bench.py --workload dense_k2_mid --steps 1
+#:       --warmup 1 --no-plain --no-cpu --no-side --no-serial --no-hbm --no-pipeline
+#: per mine 15.89 GB against 12.66 GB for the Gram, 21.26 GB against 46.00 GB for the row-major projection
+#: (its prefix rows' row words come partly from L2), 0.50 GB against 0.51 GB for the transpose; the roofline's
+#: ``traffic`` scales it to the bench's own launches by their algorithmic bytes.
+DRAM_PER_ALGORITHMIC_BYTE = {"gram_tc": 15.892 / 12.659, "project_rows": 21.262 / 45.998, "rows_transpose": 0.495 / 0.511}
 
 
 def _peaks() -> dict:
@@ -421,8 +421,31 @@ def deep_sparse_line(pkg, lib, steps: int, warmup: int, with_cpu: bool, cpu_budg
     torch.cuda.synchronize()
     ms = start.elapsed_time(end) / steps
     rep = verm.check_mine(out, bv, n_rows, generators=True, max_length=spec["max_length"], sample=10_000)
+    # End to end through apriori(bitvecs=): the 5 GB of bitvectors copied in from pinned host memory and the
+    # result frame copied back, every step.
+    host = torch.empty(bv.shape, dtype=torch.int64, pin_memory=True)
+    host.copy_(bv.view(torch.int64))
+    dev = torch.empty_like(bv.view(torch.int64))
+    col_to_item = {c: c for c in range(bv.shape[0])}
+    e2e_ms = []
+    for i in range(steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev.copy_(host, non_blocking=True)
+        df = pkg.apriori(bitvecs=(dev.view(torch.uint64), col_to_item, n_rows), min_support=spec["min_support"],
+                         max_length=spec["max_length"], use_generator_pruning=True, engine=eng, warn_complexity=False)
+        torch.cuda.synchronize()
+        if i > 0:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    n_sets = len(df)
+    del df, host, dev
     line = {"workload": "deep_sparse", "config": {**spec, "rows_generated_on": "device (etm_synth_patterns)"},
             "metric": "mine() seconds, bitvectors resident", "value": ms / 1e3, "unit": "s", "steps": steps,
+            "e2e": {"value": statistics.median(e2e_ms) / 1e3, "unit": "s", "steps_ms": [round(x, 2) for x in e2e_ms],
+                    "h2d_bytes_per_step": int(bv.numel() * 8),
+                    "d2h_bytes_per_step": int(8 * sum(lv.n * lv.k for lv in out.levels) + 8 * len(out.level1_cols)
+                                              + 16 * out.n_itemsets() + 8),
+                    "itemsets": n_sets},
             "levels": [{"k": s.k, "candidates": s.n_candidates, "frequent": s.n_frequent} for s in out.stats],
             "itemsets": out.n_itemsets(), "gpu_launches": (eng.launches - launches0) // steps,
             "exact": {"sampled": rep["sampled"], "mismatches": rep["mismatches"],
@@ -701,6 +724,9 @@ def main() -> None:
     ap.add_argument("--no-hbm", action="store_true", help="skip the AND+popcount / bitvector kernel rooflines")
     ap.add_argument("--hbm-rows-default", type=int, default=8_000_000,
                     help="transactions of the kernel-roofline input in the default line")
+    ap.add_argument("--proj-cols", action="store_true",
+                    help="project with the column form (etm_project: member segments by bulk copies) instead of the "
+                         "row-major form")
     ap.add_argument("--no-pipeline", action="store_true",
                     help="project and count chunks in turn on one stream (per-kernel times without overlap)")
     args = ap.parse_args()
@@ -753,7 +779,7 @@ def main() -> None:
     n_rows = spec["n_rows"]
     extra = {"chunk_cands": args.chunk_cands} if args.chunk_cands else {}
     eng = engm.Engine(form="batched", method=method, tc_elem=args.tc_elem, proj_bytes=int(args.proj_gb * (1 << 30)),
-                      pipeline=not args.no_pipeline, **extra)
+                      pipeline=not args.no_pipeline, proj_rows=not args.proj_cols, **extra)
     eng.profile_kernels = True
 
     def one(e):
@@ -792,7 +818,7 @@ def main() -> None:
     plain = None
     if not args.no_plain:
         pe = engm.Engine(form="plain", method=method, tc_elem=args.tc_elem, proj_bytes=int(args.proj_gb * (1 << 30)),
-                         **extra)
+                         proj_rows=not args.proj_cols, **extra)
         one(pe)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -807,7 +833,7 @@ def main() -> None:
     serial = None
     if not args.no_serial:
         se = engm.Engine(form="batched", method=method, tc_elem=args.tc_elem, proj_bytes=int(args.proj_gb * (1 << 30)),
-                         pipeline=False, **extra)
+                         pipeline=False, proj_rows=not args.proj_cols, **extra)
         se.profile_kernels = True
         one(se)
         se.reset_kernel_times()
@@ -938,7 +964,8 @@ def main() -> None:
             "exact": exact,
             "plain": plain,
             "e2e": {"value": statistics.median(e2e_ms) / 1e3, "unit": "s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "itemsets": n_items_out},
+                    "d2h_bytes_per_step": d2h, "itemsets": n_items_out,
+                    "steps_ms": [round(x, 1) for x in e2e_ms]},
             "roofline": roof,
             "rooflines": rooflines,
             "serial": serial,

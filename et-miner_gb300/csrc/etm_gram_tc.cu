@@ -279,8 +279,9 @@ __global__ void __launch_bounds__(STAGED ? ST_THREADS : THREADS, 1) gram_kernel(
     __shared__ __align__(8) uint64_t drain_bar;
     __shared__ uint32_t tmem_sh;
     __shared__ int abort_sh;
-    __shared__ int64_t off_a[256];
-    __shared__ int64_t off_b[256];
+    // Member row offsets of the block pair (the producers of the unstaged form load their rows themselves).
+    __shared__ int64_t off_a[STAGED ? 1 : 256];
+    __shared__ int64_t off_b[STAGED ? 1 : 256];
     __shared__ int64_t next_sh;
 
     uint8_t* slots = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~uintptr_t(1023));
@@ -358,7 +359,7 @@ __global__ void __launch_bounds__(STAGED ? ST_THREADS : THREADS, 1) gram_kernel(
         const int64_t cb = cand_off[g] - chunk_base;
         const int64_t words = cwords[wi];
         const int64_t n_stages = ceil_div<int64_t>(words, WORDS);
-        if (tid < 256) {
+        if (!STAGED && tid < 256) {
             const int64_t ia = a0 + tid, ib = b0 + tid;
             // Row-major rows: member i at cbase + i cld. Blocked rows (blocks of T members stored 4-word chunk
             // by chunk, each chunk as two 2-word halves, so a stage's words of one block are one run): member i
@@ -382,7 +383,7 @@ __global__ void __launch_bounds__(STAGED ? ST_THREADS : THREADS, 1) gram_kernel(
             const bool is_b = tid >= 256;
             const int prow = is_b ? tid - 256 : tid;
             const bool idle = prow >= T || (!is_b && diag);  // on a diagonal block pair the A rows are B rows
-            const int64_t off = idle ? -1 : (is_b ? off_b[prow] : off_a[prow]);
+            const int64_t off = (STAGED || idle) ? -1 : (is_b ? off_b[prow] : off_a[prow]);
             // B row r: row r of the 256-row B tile; A row r: row r % TH of A half r / TH.
             const int dst = is_b ? 2 * HALF_BYTES : (prow / TH) * HALF_BYTES;
             const int hrow = is_b ? prow : prow % TH;

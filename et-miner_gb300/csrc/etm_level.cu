@@ -332,14 +332,47 @@ struct WordSurvivors {
     __device__ int64_t operator()(int64_t w) const { return __popc(bits(w)); }
 };
 
+// The survivors of one 32-candidate word, in order. The word's first survivor is decoded in full (group by
+// binary search, (i, j) from the triangular index); each later one by walking (group, i, j) forward over the
+// candidates between them, with integer steps only: no search and no square root per survivor, which is what
+// bounds words dense in survivors.
 struct EmitWordSurvivors {
     WordSurvivors words;
     EmitSurvivor emit;
     __device__ void operator()(int64_t w, int64_t off) const {
         uint32_t b = words.bits(w);
-        while (b) {
-            emit((w << 5) + (__ffs(b) - 1), off++);
+        if (b == 0u) return;
+        int64_t pos = (w << 5) + (__ffs(b) - 1);
+        const Cand c = decode_candidate(emit.cand_off, emit.grp_size, emit.g0, emit.g1, emit.cand_off[emit.g0] + pos);
+        int64_t g = c.g, i = c.i, j = c.j;
+        int64_t m = emit.grp_size[g], first = emit.grp_first[g];
+        const int width = emit.width;
+        for (;;) {
+            if (off < emit.cap) {
+                const int32_t* ri = emit.rows + (first + i) * width;
+                int32_t* o = emit.out_rows + off * (width + 1);
+                for (int q = 0; q < width; q++) o[q] = ri[q];
+                o[width] = emit.rows[(first + j) * width + width - 1];
+                emit.out_counts[off] = emit.counts[pos];
+            }
+            ++off;
             b &= b - 1u;
+            if (b == 0u) return;
+            const int64_t next = (w << 5) + (__ffs(b) - 1);
+            for (int64_t d = next - pos; d > 0; d--) {
+                if (++j == m) {
+                    if (++i == m - 1) {  // past the group's last pair: the next group holding a pair
+                        do {
+                            ++g;
+                        } while (g + 1 < emit.g1 && emit.grp_size[g] < 2);
+                        m = emit.grp_size[g];
+                        first = emit.grp_first[g];
+                        i = 0;
+                    }
+                    j = i + 1;
+                }
+            }
+            pos = next;
         }
     }
 };

@@ -485,33 +485,51 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
 // rounds each) turn rows into columns, so lane k ends with column 32 c + k's bits at the 128 rows: two
 // projected words, stored with one 16-byte store when that column is a member of the group. Only the prefix
 // rows' words are read (a segment's prefix rows are a few per cent of its rows at the densities the
-// projection serves), where the column form reads every member's whole segment; a transpose costs under one
-// instruction per projected 32-bit word, a gather by ballots about three.
+// projection serves), where the column form reads every member's whole segment; a transpose costs about
+// half an instruction per projected 32-bit word, a gather by ballots about three.
 constexpr int RT = 256;
 constexpr int R_WARPS = RT / 32;
 constexpr int R_LIST = 8192;  // prefix rows listed per pass (128-row blocks: 64)
 
-// Lane i holds row i of a 32 x 32 bit matrix (bit k = column k); returns column `lane` (bit i = row i).
-// Round j swaps the off-diagonal j x j blocks of every 2j x 2j block (Hacker's Delight, "transpose32",
-// with the partner row taken by a shuffle).
-__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
-#pragma unroll
-    for (int j = 16; j >= 1; j >>= 1) {
-        const uint32_t m = j == 16 ? 0x0000FFFFu : j == 8 ? 0x00FF00FFu : j == 4 ? 0x0F0F0F0Fu : j == 2 ? 0x33333333u
-                                                                                                      : 0x55555555u;
-        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
-        x = (lane & j) ? ((x & ~m) | ((y >> j) & m)) : ((x & m) | ((y & m) << j));
+// Lane i holds row i of a 32 x 32 bit matrix (bit k = column k); the call returns column `lane` (bit i = row
+// i). Round j swaps the off-diagonal j x j blocks of every 2j x 2j block, with the partner row taken by a
+// shuffle (Hacker's Delight, "transpose32"): for j = 16 and 8 the swap moves whole bytes, one byte permute
+// with a per-lane selector; for j = 4, 2, 1 the partner row is rotated by j one way or the other (a funnel
+// shift by a per-lane amount) and merged under a per-lane mask (one three-input logic op). The per-lane
+// constants are set once per thread.
+struct Transpose32 {
+    uint32_t sel16, sel8, rot4, rot2, rot1, keep4, keep2, keep1;
+    __device__ explicit Transpose32(int lane) {
+        sel16 = (lane & 16) ? 0x3276u : 0x5410u;
+        sel8 = (lane & 8) ? 0x3715u : 0x6240u;
+        rot4 = (lane & 4) ? 4u : 28u;
+        rot2 = (lane & 2) ? 2u : 30u;
+        rot1 = (lane & 1) ? 1u : 31u;
+        keep4 = (lane & 4) ? ~0x0F0F0F0Fu : 0x0F0F0F0Fu;
+        keep2 = (lane & 2) ? ~0x33333333u : 0x33333333u;
+        keep1 = (lane & 1) ? ~0x55555555u : 0x55555555u;
     }
-    return x;
-}
+    __device__ __forceinline__ uint32_t operator()(uint32_t x) const {
+        x = __byte_perm(x, __shfl_xor_sync(0xffffffffu, x, 16), sel16);
+        x = __byte_perm(x, __shfl_xor_sync(0xffffffffu, x, 8), sel8);
+        uint32_t y = __shfl_xor_sync(0xffffffffu, x, 4);
+        x = (x & keep4) | (__funnelshift_r(y, y, rot4) & ~keep4);
+        y = __shfl_xor_sync(0xffffffffu, x, 2);
+        x = (x & keep2) | (__funnelshift_r(y, y, rot2) & ~keep2);
+        y = __shfl_xor_sync(0xffffffffu, x, 1);
+        x = (x & keep1) | (__funnelshift_r(y, y, rot1) & ~keep1);
+        return x;
+    }
+};
 
 __device__ __forceinline__ uint32_t u4_word(const uint4& v, int c) {
     return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w;
 }
 
-// xt [64 n_words][ldr]: one CTA per 128 rows x 256 columns; warp w transposes chunk 8 y + w of the two words
-// of its 32 columns, and the tile goes out as 32 contiguous bytes per row.
-__global__ void __launch_bounds__(RT) rows_transpose_kernel(const uint64_t* __restrict__ fbv, int64_t ld,
+// xt [64 n_words][ldr]: one CTA of 256 threads per 128 rows x 256 columns; warp w transposes chunk 8 y + w of
+// the two words of its 32 columns, and the tile goes out as 32 contiguous bytes per row (two threads a row).
+constexpr int XT_THREADS = 256;
+__global__ void __launch_bounds__(XT_THREADS) rows_transpose_kernel(const uint64_t* __restrict__ fbv, int64_t ld,
                                                            int64_t n_words, int64_t n_cols,
                                                            uint32_t* __restrict__ xt, int64_t ldr) {
     __shared__ uint32_t tile[128][9];
@@ -524,10 +542,11 @@ __global__ void __launch_bounds__(RT) rows_transpose_kernel(const uint64_t* __re
         a = __ldg(fbv + col * ld + w);
         if (w + 1 < n_words) b = __ldg(fbv + col * ld + w + 1);
     }
-    tile[lane][warp] = transpose32((uint32_t)a, lane);
-    tile[32 + lane][warp] = transpose32((uint32_t)(a >> 32), lane);
-    tile[64 + lane][warp] = transpose32((uint32_t)b, lane);
-    tile[96 + lane][warp] = transpose32((uint32_t)(b >> 32), lane);
+    const Transpose32 tp(lane);
+    tile[lane][warp] = tp((uint32_t)a);
+    tile[32 + lane][warp] = tp((uint32_t)(a >> 32));
+    tile[64 + lane][warp] = tp((uint32_t)b);
+    tile[96 + lane][warp] = tp((uint32_t)(b >> 32));
     __syncthreads();
     const int r = threadIdx.x >> 1, h = threadIdx.x & 1;
     const int64_t row = w * 64 + r;
@@ -551,6 +570,7 @@ __global__ void __launch_bounds__(RT, 3) project_rows_kernel(
     int32_t* cgl = crank + ldr;                                       // 4-chunk groups holding a member
     __shared__ int32_t pref[64];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const Transpose32 tp(lane);
     const int plen = width - 1;
     const int64_t total = n_seg * n_work;
     // Units round-robin in segment-major order (CTA b takes b, b + grid, ...): the units are many and small, and
@@ -651,10 +671,10 @@ __global__ void __launch_bounds__(RT, 3) project_rows_kernel(
                 for (int cc = 0; cc < 4; cc++) {
                     const uint32_t mk = cmask[cg + cc];
                     if (mk == 0u) continue;  // warp-uniform
-                    const uint32_t t0 = transpose32(u4_word(v[0], cc), lane);
-                    const uint32_t t1 = transpose32(u4_word(v[1], cc), lane);
-                    const uint32_t t2 = transpose32(u4_word(v[2], cc), lane);
-                    const uint32_t t3 = transpose32(u4_word(v[3], cc), lane);
+                    const uint32_t t0 = tp(u4_word(v[0], cc));
+                    const uint32_t t1 = tp(u4_word(v[1], cc));
+                    const uint32_t t2 = tp(u4_word(v[2], cc));
+                    const uint32_t t3 = tp(u4_word(v[3], cc));
                     if ((mk >> lane) & 1u) {
                         const int64_t i = crank[cg + cc] + __popc(mk & ((1u << lane) - 1u));
                         *reinterpret_cast<ulonglong2*>(dst + proj_member_offset(i, stride, blk) + wo) =
@@ -794,7 +814,7 @@ extern "C" int etm_rows_transpose(const uint64_t* fbv, int64_t ld, int64_t n_wor
     ETM_REQUIRE(n_words < (1LL << 32) && ldr / 8 < 65535, ETM_EINVAL, "etm_rows_transpose: too large");
     if (n_words == 0 || ldr == 0) return ETM_OK;
     const dim3 grid((unsigned)ceil_div<int64_t>(n_words, 2), (unsigned)ceil_div<int64_t>(ldr, 8));
-    rows_transpose_kernel<<<grid, RT, 0, as_stream(stream)>>>(fbv, ld, n_words, n_cols, xt, ldr);
+    rows_transpose_kernel<<<grid, XT_THREADS, 0, as_stream(stream)>>>(fbv, ld, n_words, n_cols, xt, ldr);
     ETM_LAUNCHED("rows_transpose");
     return ETM_OK;
 }

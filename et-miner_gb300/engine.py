@@ -26,7 +26,9 @@ Forms:
 from __future__ import annotations
 
 import math
+import threading
 import time
+import weakref
 from dataclasses import dataclass, field
 from fractions import Fraction
 
@@ -220,20 +222,60 @@ class MineOutput:
 PINNED_RESULT_BYTES = 64 << 20
 
 
+class _PinnedPool:
+    """Page-locked host buffers for results, shared by the engines of the process. A buffer is handed out again
+    only once every numpy array made from it has been dropped (weak references), so a result never shares
+    memory with a live earlier result, and steady-state calls pin nothing new; at most ``max_buffers`` are
+    kept (past that, results come back through pageable memory)."""
+
+    def __init__(self, max_buffers: int = 4):
+        self.lock = threading.Lock()
+        self.entries: list[list] = []  # [uint8 page-locked tensor, [weak references or a busy marker]]
+        self.max_buffers = max_buffers
+
+    @staticmethod
+    def _free(entry) -> bool:
+        return all(r() is None for r in entry[1])
+
+    def arrays(self, tensors: list[torch.Tensor]) -> list[np.ndarray] | None:
+        sizes = [t.numel() * t.element_size() for t in tensors]
+        offs, total = [], 0
+        for n in sizes:
+            offs.append(total)
+            total += -(-n // 256) * 256
+        with self.lock:
+            entry = next((e for e in self.entries if e[0].numel() >= total and self._free(e)), None)
+            if entry is None:
+                if len(self.entries) >= self.max_buffers:
+                    free = [e for e in self.entries if self._free(e)]
+                    if not free:
+                        return None
+                    self.entries.remove(free[0])
+                entry = [torch.empty(total, dtype=torch.uint8, pin_memory=True), []]
+                self.entries.append(entry)
+            entry[1] = [lambda: True]  # busy while the copies run
+        buf = entry[0]
+        views = [buf[o:o + n].view(t.dtype).view(t.shape) for o, n, t in zip(offs, sizes, tensors)]
+        for v, t in zip(views, tensors):
+            v.copy_(t, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        out = [v.numpy() for v in views]
+        with self.lock:
+            entry[1] = [weakref.ref(a) for a in out]
+        return out
+
+
+_PINNED = _PinnedPool()
+
+
 def _copy_to_host(*tensors: torch.Tensor) -> list[np.ndarray]:
-    """Device tensors as host numpy arrays. Large results are copied into page-locked tensors from torch's
-    caching host allocator (full-rate copies, no page faults on fresh memory; a block returns to the cache when
-    the arrays viewing it are dropped, so repeated calls reuse it); small ones go through ``.cpu()``."""
-    big = sum(t.numel() * t.element_size() for t in tensors) >= PINNED_RESULT_BYTES
-    if not big:
-        return [t.cpu().numpy() for t in tensors]
-    hosts = []
-    for t in tensors:
-        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
-        h.copy_(t, non_blocking=True)
-        hosts.append(h)
-    torch.cuda.current_stream().synchronize()
-    return [h.numpy() for h in hosts]
+    """Device tensors as host numpy arrays: large results through the page-locked pool (full-rate copies, no
+    page faults on fresh memory), small ones (or with the pool exhausted) through ``.cpu()``."""
+    if sum(t.numel() * t.element_size() for t in tensors) >= PINNED_RESULT_BYTES:
+        got = _PINNED.arrays(list(tensors))
+        if got is not None:
+            return got
+    return [t.cpu().numpy() for t in tensors]
 
 
 class _Scratch:
@@ -339,7 +381,8 @@ class Engine:
         if (int(tc_elem) & ~TC_WIDE) not in (1, 2, TC_MXF4):
             raise ValueError(f"tc_elem must be 1 (e4m3), 2 (f16) or 4 (e2m1), optionally | 16; got {tc_elem}")
         self.tc_elem = int(tc_elem)
-        #: Batched form: project chunk c+1 on a side stream while chunk c is counted.
+        #: Batched form with the column projection (proj_rows=False): project chunk c+1 on a side stream while
+        #: chunk c is counted.
         self.pipeline = bool(pipeline)
         #: Fused threshold: the counting kernels write only the counts reaching min_count and a survivor bit each;
         #: compaction scans the bitmask (a 32nd of the dense counts). False: dense counts, dense compaction.
@@ -734,9 +777,11 @@ class Engine:
             g0 = g1
         # The row-major copy for the projection, made on the main stream before any side-stream work reads it.
         xt = self._rows_copy(fbv, ldp, n_words) if (self.proj_rows and proj.any()) else None
-        # Batched form: the projection of chunk c+1 runs on a side stream while chunk c is counted
-        # (memory-bound gathers beside tensor-bound MMAs); two scratch sets alternate.
-        pipelined = self.pipeline and self.form == "batched" and proj.any()
+        # Batched form with the column projection: the projection of chunk c+1 runs on a side stream while chunk
+        # c is counted; two scratch sets alternate. The row-major projection stays on the main stream: it is
+        # short, and the Gram's CTAs leave no room on their SMs for it (measured: 0.563 s per dense K=2 mine
+        # with the side stream, 0.545 s without).
+        pipelined = self.pipeline and self.form == "batched" and proj.any() and xt is None
         main = torch.cuda.current_stream()
         side = self._side_stream() if pipelined else None
         prep_done = [torch.cuda.Event(), torch.cuda.Event()]
@@ -929,7 +974,11 @@ class Engine:
                 new_total = int(acc.item())
                 if new_total <= cap:
                     break
-                cap = int(min(total, max(2 * cap, int(new_total * 1.25))))
+                # Grow to the level's survivors extrapolated from the candidates counted so far, so that the
+                # later chunks compact once.
+                done = max(1, int(offs[g1] - offs[0]))
+                projected = int(new_total * (total / done) * 1.1)
+                cap = int(min(total, max(2 * cap, int(new_total * 1.25), projected)))
                 grown_r = torch.empty((cap, width + 1), dtype=torch.int32, device=self.device)
                 grown_c = torch.empty(cap, dtype=torch.int32, device=self.device)
                 grown_r[:n_out] = out_rows[:n_out]

@@ -297,3 +297,26 @@ def test_deduction_bounds_skip_a_candidate_inference_cannot_settle(pkg):
         assert miner.canonical([(c, n) for c, n in out.host_levels()]) == miner.canonical(ref.levels)
         skipped[bounds] = sum(st.n_skipped for st in out.stats)
     assert skipped == {False: 0, True: 1}
+
+
+def test_page_locked_results_never_alias_live_ones(pkg, monkeypatch):
+    """Results copied back through the page-locked pool: a later call never writes into the buffers of a result
+    still alive, and a dropped result's buffer is used again."""
+    from importlib import import_module
+
+    engm = import_module(pkg.__name__ + ".engine")
+    monkeypatch.setattr(engm, "PINNED_RESULT_BYTES", 0)
+    syn = pkg.synthetic
+    t1 = syn.plain_small(n_rows=5_000, n_items=200, seed=11)
+    t2 = syn.plain_small(n_rows=7_000, n_items=300, seed=12)
+    a = pkg.apriori(table_of(t1.indptr, t1.items, t1.n_rows), min_support=0.01, use_gpu=True, warn_complexity=False)
+    pairs_a = pkg.result_pairs(a, t1.n_rows)
+    b = pkg.apriori(table_of(t2.indptr, t2.items, t2.n_rows), min_support=0.01, use_gpu=True, warn_complexity=False)
+    assert pkg.result_pairs(a, t1.n_rows) == pairs_a
+    ref, items = miner.mine_transactions(t2.indptr, t2.items, t2.n_rows, 0.01)
+    assert pkg.result_pairs(b, t2.n_rows) == miner.canonical(ref.levels, items)
+    n_buffers = len(engm._PINNED.entries)
+    del a
+    c = pkg.apriori(table_of(t1.indptr, t1.items, t1.n_rows), min_support=0.01, use_gpu=True, warn_complexity=False)
+    assert pkg.result_pairs(c, t1.n_rows) == pairs_a
+    assert len(engm._PINNED.entries) == n_buffers  # the dropped result's buffer served the new one
