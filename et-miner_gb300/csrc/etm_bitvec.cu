@@ -44,39 +44,38 @@ __global__ void __launch_bounds__(BUILD_THREADS) build_bitvecs_kernel(
 }
 
 // Shared-memory form for up to SMEM_BUILD_COLS columns: the block's 256 rows are 4 words of every column,
-// held in shared memory (n_cols x 32 bytes); entries OR their bits there, then the block writes each of its
-// words once, 32 contiguous bytes per column. Every output word is written by exactly one block, so the
+// held in shared memory as [word][column] (n_cols x 32 bytes); each warp takes whole rows (a row's entries are
+// distinct columns, so a warp's ORs hit distinct words, spread over the banks), then the block writes each of
+// its words once, 32 contiguous bytes per column. Every output word is written by exactly one block, so the
 // output needs no zeroing first and no global atomics run.
 constexpr int SMEM_BUILD_COLS = 3072;  // 96 KB of shared memory
 __global__ void __launch_bounds__(BUILD_THREADS) build_bitvecs_smem_kernel(
     const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ ids, int64_t nnz, const int32_t* __restrict__ lut,
     int64_t lut_size, int64_t n_rows, int64_t n_cols, int64_t ld, uint64_t* __restrict__ out) {
-    extern __shared__ unsigned long long words[];  // [n_cols][4]
+    extern __shared__ unsigned long long words[];  // [4][n_cols]
     __shared__ int64_t ptr[BUILD_ROWS + 1];
     const int64_t r0 = (int64_t)blockIdx.x * BUILD_ROWS;
     const int nr = (int)min64(BUILD_ROWS, n_rows - r0);
     for (int t = threadIdx.x; t <= nr; t += blockDim.x) ptr[t] = row_ptr[r0 + t];
     for (int64_t t = threadIdx.x; t < n_cols * 4; t += blockDim.x) words[t] = 0ULL;
     __syncthreads();
-    const int64_t e0 = max64(ptr[0], 0), e1 = min64(ptr[nr], nnz);
-    for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        int lo = 0, hi = nr;
-        while (hi - lo > 1) {
-            int mid = (lo + hi) >> 1;
-            if (ptr[mid] <= e) lo = mid;
-            else hi = mid;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
+    for (int r = warp; r < nr; r += n_warps) {
+        const int64_t b = max64(ptr[r], 0), e = min64(ptr[r + 1], nnz);
+        unsigned long long* wq = words + (int64_t)(r >> 6) * n_cols;
+        const unsigned long long bit = 1ULL << (r & 63);
+        for (int64_t i = b + lane; i < e; i += 32) {
+            int64_t col = ids[i];
+            if (lut) col = (col >= 0 && col < lut_size) ? (int64_t)lut[col] : -1;
+            if (col < 0 || col >= n_cols) continue;
+            atomicOr(wq + col, bit);
         }
-        if (e < ptr[lo] || e >= ptr[lo + 1]) continue;
-        int64_t col = ids[e];
-        if (lut) col = (col >= 0 && col < lut_size) ? (int64_t)lut[col] : -1;
-        if (col < 0 || col >= n_cols) continue;
-        atomicOr(words + col * 4 + (lo >> 6), 1ULL << (lo & 63));
     }
     __syncthreads();
     const int64_t w0 = r0 >> 6;
     for (int64_t t = threadIdx.x; t < n_cols * 4; t += blockDim.x) {
-        const int64_t w = w0 + (t & 3);
-        if (w < ld) out[(t >> 2) * ld + w] = words[t];
+        const int64_t col = t >> 2, q = t & 3;
+        if (w0 + q < ld) out[col * ld + w0 + q] = words[q * n_cols + col];
     }
 }
 

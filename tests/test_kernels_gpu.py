@@ -27,13 +27,16 @@ def _dev(a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
-@pytest.mark.parametrize("n_rows", [1, 63, 64, 65, 1000, 100_003])
-def test_build_bitvecs_is_byte_identical(pkg, lib, n_rows):
+@pytest.mark.parametrize("n_rows,n_items,max_len", [(1, 37, 12), (63, 37, 12), (64, 37, 12), (65, 37, 12),
+                                                    (1000, 37, 12), (100_003, 37, 12), (20_011, 3000, 90),
+                                                    (3_001, 5000, 70)])
+def test_build_bitvecs_is_byte_identical(pkg, lib, n_rows, n_items, max_len):
+    """The shared-memory form (up to 3,072 columns; rows longer than a warp) and the global form, against the
+    host restatement."""
     import torch
 
-    rng = np.random.default_rng(n_rows)
-    n_items = 37
-    lens = rng.integers(0, 12, n_rows)
+    rng = np.random.default_rng(n_rows + n_items)
+    lens = rng.integers(0, max_len, n_rows)
     indptr = np.zeros(n_rows + 1, np.int64)
     np.cumsum(lens, out=indptr[1:])
     rows = [np.sort(rng.choice(n_items, size=l, replace=False)) for l in lens]
