@@ -25,6 +25,7 @@ Forms:
 
 from __future__ import annotations
 
+import gc
 import math
 import threading
 import time
@@ -245,6 +246,11 @@ class _PinnedPool:
             total += -(-n // 256) * 256
         with self.lock:
             entry = next((e for e in self.entries if e[0].numel() >= total and self._free(e)), None)
+            if entry is None and self.entries:
+                # A dropped result held in a reference cycle is freed only by the collector: collect once before
+                # pinning another buffer (pinning several GB takes longer than a collection).
+                gc.collect()
+                entry = next((e for e in self.entries if e[0].numel() >= total and self._free(e)), None)
             if entry is None:
                 if len(self.entries) >= self.max_buffers:
                     free = [e for e in self.entries if self._free(e)]
