@@ -245,12 +245,14 @@ class _PinnedPool:
             offs.append(total)
             total += -(-n // 256) * 256
         with self.lock:
+            have = any(e[0].numel() >= total and self._free(e) for e in self.entries)
+            busy = bool(self.entries)
+        if not have and busy:
+            # A dropped result held in a reference cycle is freed only by the collector: collect once (outside
+            # the lock: finalizers may run) before pinning another buffer, which takes longer than a collection.
+            gc.collect()
+        with self.lock:
             entry = next((e for e in self.entries if e[0].numel() >= total and self._free(e)), None)
-            if entry is None and self.entries:
-                # A dropped result held in a reference cycle is freed only by the collector: collect once before
-                # pinning another buffer (pinning several GB takes longer than a collection).
-                gc.collect()
-                entry = next((e for e in self.entries if e[0].numel() >= total and self._free(e)), None)
             if entry is None:
                 if len(self.entries) >= self.max_buffers:
                     free = [e for e in self.entries if self._free(e)]

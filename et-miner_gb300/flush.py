@@ -197,7 +197,8 @@ class _Writer:
         self.items, self.sup, self.codec = items, sup, codec
 
     def _page(self, num_values: int, body: bytes, levels: bool) -> tuple[bytes, int, int]:
-        payload = gzip.compress(body, compresslevel=6) if self.codec == "gzip" else body
+        # Level 1: the fast end, like the reference's zstd level 2 (a level can be megabytes to gigabytes).
+        payload = gzip.compress(body, compresslevel=1) if self.codec == "gzip" else body
         dph = _Struct().i32(1, num_values).i32(2, _PLAIN).i32(3, _RLE).i32(4, _RLE)
         header = _Struct().i32(1, 0).i32(2, len(body)).i32(3, len(payload)).struct(5, dph).end()
         return header + payload, len(header) + len(body), len(header) + len(payload)
