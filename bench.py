@@ -713,7 +713,7 @@ def main() -> None:
                     help="tensor operands: 1 = e4m3, 2 = f16, 4 = packed e2m1 (kind::mxf4); + 16 is ignored "
                          "(default: the engine's)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparator")
-    ap.add_argument("--proj-gb", type=float, default=8.0, help="device GB of projected words per chunk")
+    ap.add_argument("--proj-gb", type=float, default=16.0, help="device GB of projected words per chunk")
     ap.add_argument("--chunk-cands", type=int, default=None, help="candidates per chunk (default: the engine's)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU route runs")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds the CPU baseline mine may run")

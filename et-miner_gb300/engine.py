@@ -45,12 +45,12 @@ SMALL_GROUP = 16
 #: Suffixes per tile side of the tile-pair kernel.
 TILE = 64
 #: Candidates per chunk (int32 count + uint8 class each): bounds the level's dense scratch.
-CHUNK_CANDS = 1 << 28
+CHUNK_CANDS = 1 << 29
 #: A group of more than SMALL_GROUP members is counted on its prefix's rows only when the prefix
 #: holds less than this fraction of the transactions.
 PROJ_DENSITY = 0.5
 #: Device bytes of projected suffix words per chunk (two such sets alternate between the streams).
-PROJ_BYTES = 8 << 30
+PROJ_BYTES = 16 << 30
 #: Members per block of the tensor-core Gram kernel (e4m3 and f16 operands; packed e2m1 blocks hold 240):
 #: a block pair (ua <= ub) is one work item.
 TC_TILE = 256
