@@ -390,7 +390,9 @@ __global__ void __launch_bounds__(STAGED ? ST_THREADS : THREADS, 1) gram_kernel(
             if constexpr (STAGED) {
                 // Raw bits from the loader's ring (A block at 0, B block at RAW_BLOCK of a slot): wait for the
                 // slot, read this row's two 16-byte halves (words 0-1 at 16 prow, words 2-3 at 16 (T + prow):
-                // a warp reads two contiguous 512-byte runs), release the slot, then expand into the stage.
+                // a warp reads two contiguous 512-byte runs), expand them into the stage, then release the slot.
+                // The release comes after the expansion has consumed the loaded words, so the loader's next
+                // bulk copy into the slot (async proxy) cannot land before these reads (generic proxy) are done.
                 const bool skip = idle || (is_b ? b0 : a0) + prow >= m;
                 const int raw_off = (is_b ? RAW_BLOCK : 0) + prow * 16;
                 for (int64_t s = 0; s < n_stages; s++) {
@@ -409,13 +411,13 @@ __global__ void __launch_bounds__(STAGED ? ST_THREADS : THREADS, 1) gram_kernel(
                         x[2] = (uint64_t)v1.x | ((uint64_t)v1.y << 32);
                         x[3] = (uint64_t)v1.z | ((uint64_t)v1.w << 32);
                     }
-                    mbar_arrive(&raw_empty[rs]);
                     if (!mbar_wait(&empty_bar[os], (ouse & 1u) ^ 1u, abort_flag, WAIT_NS)) break;
                     if (!skip) {
                         store_row<FMT>(slots + os * SLOT_BYTES + dst, hrow, x);
                         fence_proxy_async();
                     }
                     mbar_arrive(&full_bar[os]);
+                    mbar_arrive(&raw_empty[rs]);
                 }
             } else {
                 uint64_t cur[BW], nxt[BW];
