@@ -91,6 +91,9 @@ SIGNATURES: dict[str, tuple] = {
     "etm_build_bitvecs": (ctypes.c_int, [_P, _P, _I64, _P, _I64, _I64, _I64, _I64, _P, _P]),
     "etm_popcount_cols": (ctypes.c_int, [_P, _I64, _I64, _I64, _P, _P]),
     "etm_gather_cols": (ctypes.c_int, [_P, _I64, _P, _I32, _I64, _P, _I64, _P]),
+    "etm_row_order_keys": (ctypes.c_int, [_P, _P, _I64, _P, _I64, _P, _P, _P]),
+    "etm_permute_rows": (ctypes.c_int, [_P, _P, _I64, _P, _I64, _P, _P, _P, _P]),
+    "etm_tile_occupancy": (ctypes.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P]),
     "etm_synth_bernoulli": (ctypes.c_int, [_P, _I32, _I64, _U64, _P, _I64, _P]),
     "etm_synth_patterns": (ctypes.c_int, [_P, _I32, _P, _I32, _P, _P, _I32, _U64, _I32, _I64, _U64, _P, _I64, _P]),
     "etm_level_groups": (ctypes.c_int, [_P, _I64, _I32, _P, _P, _P, _P, _P, _I64, _P]),
@@ -100,9 +103,9 @@ SIGNATURES: dict[str, tuple] = {
     "etm_triple_counts_rows": (ctypes.c_int, [_P, _P, _I64, _P, _I64, _I64, _P, _P, _I64, _P, _P, _P, _I64, _I64, _P,
                                               _P, _P]),
     "etm_pair_counts_rows": (ctypes.c_int, [_P, _P, _I64, _P, _I64, _I64, _I64, _P, _P]),
-    "etm_prefix_counts": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _I64, _P, _P]),
+    "etm_prefix_counts": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _I64, _P, _P, _I64, _P]),
     "etm_prefix_rows": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _I64, _P, _P, _P]),
-    "etm_prefix_segments": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _I64, _P, _P, _P]),
+    "etm_prefix_segments": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _I64, _P, _P, _P, _I64, _P]),
     "etm_project": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "etm_project_blocked": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _I64, _P, _P, _P, _I64, _P, _P, _P]),
     "etm_rows_transpose": (ctypes.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P]),
@@ -124,7 +127,7 @@ SIGNATURES: dict[str, tuple] = {
     "etm_count_tiles_sel": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P,
                                            _P]),
     "etm_count_cands_sel": (ctypes.c_int, [_P, _I64, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P,
-                                           _P]),
+                                           _P, _I64, _P]),
     "etm_count_tiles_proj_sel": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _P, _I32, _P, _P, _P]),
     "etm_classify_sel": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _P, _P, _I64, _I64, _I32, _I32, _P, _I64, _P, _P,
                                         _I64, _P, _I64, _P, _P, _P, _P]),

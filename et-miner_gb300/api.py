@@ -255,7 +255,7 @@ def _frequent_csr(indptr: np.ndarray, flat: np.ndarray, n_rows: int, mc: int):
 
 def _frequent_csr_device(indptr: np.ndarray, flat: np.ndarray, n_rows: int, mc: int, device):
     """``_frequent_csr`` on the device: (row_ptr int64 [n_rows+1] and column ids int32 as device tensors, the
-    items of the columns and the rows' lengths on the host).
+    items of the columns, the rows' lengths and the columns' supports on the host).
 
     The same steps as the host version (sort the ids, drop repeated (row, item) pairs, keep the items
     with count >= mc, number them in ascending id order), with device sorts; UInt64 ids are sorted
@@ -288,7 +288,66 @@ def _frequent_csr_device(indptr: np.ndarray, flat: np.ndarray, n_rows: int, mc: 
     if wide:
         kept = kept ^ sign
     kept_h = kept.cpu().numpy()
-    return row_ptr, cols, (kept_h.view(np.uint64) if wide else kept_h), row_len.cpu().numpy()
+    return (row_ptr, cols, (kept_h.view(np.uint64) if wide else kept_h), row_len.cpu().numpy(),
+            counts[keep].cpu().numpy())
+
+
+#: Device bytes per row the lex row order holds at its peak (two int64 keys, the sort's keys, indices and
+#: buffers, the permuted lengths and offsets), plus 4 per entry for the permuted columns; without them free the
+#: rows keep their order (gpu/input_layer.py:56-58, 500-529).
+LEX_BYTES_PER_ROW = 96
+
+
+def _lex_order(row_ptr, cols, support: np.ndarray):
+    """A device CSR of columns with its rows in the lex row order (gpu/input_layer.py:408-430): sorted by the
+    ranks of their most frequent columns (etm_row_order_keys, then a stable sort by the low key and one by
+    the high key), the entries moved by etm_permute_rows. Rows sharing their frequent columns gather, so
+    deep itemsets' rows fill few tiles and the tile occupancy skips the rest; counts do not depend on the
+    order. Returns (row_ptr, cols, host row lengths), or None when the order does not fit on the device.
+
+    Ranks follow descending support, ties by column (the reference ranks by occurrences, repeats included;
+    the order differs only where a row repeats an item and never changes a count).
+    """
+    import torch
+
+    from ._lib import check, load_library
+
+    n_rows = int(row_ptr.numel()) - 1
+    n_cols = len(support)
+    nnz = int(cols.numel())
+    dev = row_ptr.device
+    if n_rows < 2 or n_cols == 0 or nnz == 0:
+        return None
+    free, _ = torch.cuda.mem_get_info(dev)
+    if LEX_BYTES_PER_ROW * n_rows + 4 * nnz > free:
+        return None
+    lib = load_library()
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    rank = np.empty(n_cols, np.int32)
+    rank[np.argsort(-np.asarray(support, np.int64), kind="stable")] = np.arange(n_cols, dtype=np.int32)
+    try:
+        rank_d = torch.from_numpy(rank).to(dev)
+        key_hi = torch.empty(n_rows, dtype=torch.int64, device=dev)
+        key_lo = torch.empty(n_rows, dtype=torch.int64, device=dev)
+        check(lib.etm_row_order_keys(row_ptr.data_ptr(), cols.data_ptr(), n_rows, rank_d.data_ptr(), n_cols,
+                                     key_hi.data_ptr(), key_lo.data_ptr(), stream), "etm_row_order_keys")
+        order = torch.argsort(key_lo, stable=True)
+        order = order[torch.argsort(key_hi[order], stable=True)]
+        del key_hi, key_lo
+        lens = (row_ptr[1:] - row_ptr[:-1])[order]
+        new_ptr = torch.zeros(n_rows + 1, dtype=torch.int64, device=dev)
+        torch.cumsum(lens, 0, out=new_ptr[1:])
+        new_cols = torch.empty_like(cols)
+        status = torch.zeros(1, dtype=torch.int32, device=dev)
+        check(lib.etm_permute_rows(row_ptr.data_ptr(), cols.data_ptr(), nnz, order.data_ptr(), n_rows,
+                                   new_ptr.data_ptr(), new_cols.data_ptr(), status.data_ptr(), stream),
+              "etm_permute_rows")
+        if int(status.item()) != 0:
+            raise RuntimeError("etm_permute_rows: the row order is not a permutation of the rows")
+        return new_ptr, new_cols, lens.cpu().numpy()
+    except torch.cuda.OutOfMemoryError:
+        # The free-memory check reads the device once; the sort's buffers can still miss: keep the order.
+        return None
 
 
 def _bitvecs_of_device_csr(row_ptr, cols, n_cols: int, n_rows: int):
@@ -658,10 +717,14 @@ def apriori(
         raise ValueError(f"n_transactions={n_rows:,} exceeds int32 max")
     wide = np.dtype(kind) == np.uint64
     mc = min_count(min_support, n_rows)
-    row_ptr, cols, items, row_len = _frequent_csr_device(indptr, flat, n_rows, mc, eng.device)
+    row_ptr, cols, items, row_len, support = _frequent_csr_device(indptr, flat, n_rows, mc, eng.device)
     if len(items) == 0:
         df = _frame([], max(1, n_rows), wide)
         return (df, session) if profile else df
+    # The lex row order, and with it the tile-occupancy skip (core/apriori.py:627-640, gpu/row_split.py:397-413).
+    lex = _lex_order(row_ptr, cols, support) if eng.row_order == "lex" and n_rows >= eng.lex_min_rows else None
+    if lex is not None:
+        row_ptr, cols, row_len = lex
     bv = _bitvecs_of_device_csr(row_ptr, cols, len(items), n_rows)
     rows = (row_ptr, cols, row_len)
     max_tx = int(np.diff(indptr).max()) if n_rows else 0
@@ -669,7 +732,8 @@ def apriori(
     col_items = items.astype(np.uint64 if wide else np.int64)
     out = _mine_to(eng, bv, n_rows, min_support, eff if eff >= 1 else 1, col_items, output_dir, resume_k,
                    prune_equal_support=prune_equal_support, use_generator_pruning=use_generator_pruning,
-                   level_callback=level_callback, rows=rows, max_ram_gb=max_ram_gb, max_vram_gb=max_vram_gb)
+                   level_callback=level_callback, rows=rows, max_ram_gb=max_ram_gb, max_vram_gb=max_vram_gb,
+                   occupancy=lex is not None)
     if warn_complexity and out.stats:
         _warn_complexity(out.stats[0].n_frequent, min_support)
     df = _emit(out, col_items, labels) if output_dir is None else _frame([], max(1, n_rows), wide)

@@ -194,7 +194,8 @@ __global__ void __launch_bounds__(CAND_THREADS) count_cands_kernel(
     const uint64_t* __restrict__ fbv, int64_t ld, int64_t n_words, const int32_t* __restrict__ rows, int width,
     const int64_t* __restrict__ grp_first, const int32_t* __restrict__ grp_size, const int64_t* __restrict__ cand_off,
     const int64_t* __restrict__ work_groups, const int64_t* __restrict__ work_off, int64_t n_work, int64_t chunk_base,
-    const uint8_t* __restrict__ cls, int32_t* __restrict__ out, int32_t min_count, uint32_t* __restrict__ surv) {
+    const uint8_t* __restrict__ cls, int32_t* __restrict__ out, int32_t min_count, uint32_t* __restrict__ surv,
+    const uint64_t* __restrict__ occ, int64_t occ_ld) {
     __shared__ int32_t cols_sh[CAND_THREADS / 32][MAXK];
     const int lane = threadIdx.x & 31;
     int32_t* cols = cols_sh[threadIdx.x >> 5];
@@ -217,14 +218,27 @@ __global__ void __launch_bounds__(CAND_THREADS) count_cands_kernel(
             cols[q] = q < width ? rows[(first + i) * width + q] : rows[(first + j) * width + width - 1];
         __syncwarp();
         unsigned s = 0;
-        for (int64_t v = lane; v < n_vec; v += 32) {
-            ulonglong2 x = __ldg(reinterpret_cast<const ulonglong2*>(fbv + (int64_t)cols[0] * ld) + v);
-            for (int q = 1; q < k; q++) {
-                const ulonglong2 y = __ldg(reinterpret_cast<const ulonglong2*>(fbv + (int64_t)cols[q] * ld) + v);
-                x.x &= y.x;
-                x.y &= y.y;
+        // Blocks of 64 occupancy tiles (1,024 pairs of words): with the occupancy, a tile where one of the
+        // columns holds no row is not read (pair v lies in tile v / 16), and a block with none is skipped by
+        // the whole warp.
+        for (int64_t v0 = 0; v0 < n_vec; v0 += 32 * ETM_OCC_TILE_WORDS) {
+            uint64_t live = ~0ULL;
+            if (occ != nullptr) {
+                const int64_t ow = v0 / (32 * ETM_OCC_TILE_WORDS);
+                for (int q = 0; q < k; q++) live &= __ldg(occ + (int64_t)cols[q] * occ_ld + ow);
+                if (live == 0ULL) continue;
             }
-            s += __popcll(x.x) + __popcll(x.y);
+            const int64_t v1 = min64(n_vec, v0 + 32 * ETM_OCC_TILE_WORDS);
+            for (int64_t v = v0 + lane; v < v1; v += 32) {
+                if (((live >> ((v - v0) >> 4)) & 1ULL) == 0ULL) continue;
+                ulonglong2 x = __ldg(reinterpret_cast<const ulonglong2*>(fbv + (int64_t)cols[0] * ld) + v);
+                for (int q = 1; q < k; q++) {
+                    const ulonglong2 y = __ldg(reinterpret_cast<const ulonglong2*>(fbv + (int64_t)cols[q] * ld) + v);
+                    x.x &= y.x;
+                    x.y &= y.y;
+                }
+                s += __popcll(x.x) + __popcll(x.y);
+            }
         }
         s = __reduce_add_sync(0xffffffffu, s);
         if (lane == 0) emit_count(out, surv, t, (int32_t)s, min_count);
@@ -331,7 +345,8 @@ extern "C" int etm_count_cands(const uint64_t* fbv, int64_t ld, int64_t n_words,
     const int grid = max(1, sm_count()) * 8;
     count_cands_kernel<<<grid, CAND_THREADS, 0, as_stream(stream)>>>(fbv, ld, n_words, rows, width, grp_first, grp_size,
                                                                      cand_off, work_groups, work_off, n_work,
-                                                                     chunk_base, cls, out_counts, 0, nullptr);
+                                                                     chunk_base, cls, out_counts, 0, nullptr, nullptr,
+                                                                     0);
     ETM_LAUNCHED("count_cands");
     return ETM_OK;
 }
@@ -340,8 +355,11 @@ extern "C" int etm_count_cands_sel(const uint64_t* fbv, int64_t ld, int64_t n_wo
                                    int32_t width, const int64_t* grp_first, const int32_t* grp_size,
                                    const int64_t* cand_off, const int64_t* work_groups, const int64_t* work_off,
                                    int64_t n_work, int64_t chunk_base, const uint8_t* cls, int32_t min_count,
-                                   int32_t* out_counts, uint32_t* surv_bits, void* stream) {
+                                   int32_t* out_counts, uint32_t* surv_bits, const uint64_t* occ, int64_t occ_ld,
+                                   void* stream) {
     ETM_REQUIRE(width >= 1 && width < MAXK, ETM_EINVAL, "etm_count_cands_sel: width %d out of range", width);
+    ETM_REQUIRE(occ == nullptr || occ_ld >= ceil_div<int64_t>(ceil_div<int64_t>(n_words, ETM_OCC_TILE_WORDS), 64),
+                ETM_EINVAL, "etm_count_cands_sel: occ_ld too small for n_words");
     ETM_REQUIRE(ld % 2 == 0 && ld >= n_words, ETM_EINVAL, "etm_count_cands_sel: ld must be even and >= n_words");
     ETM_REQUIRE((reinterpret_cast<uintptr_t>(fbv) & 15) == 0, ETM_EINVAL, "etm_count_cands_sel: fbv must be 16-byte aligned");
     ETM_REQUIRE(surv_bits != nullptr, ETM_EINVAL, "etm_count_cands_sel: surv_bits is required");
@@ -349,7 +367,8 @@ extern "C" int etm_count_cands_sel(const uint64_t* fbv, int64_t ld, int64_t n_wo
     const int grid = max(1, sm_count()) * 8;
     count_cands_kernel<<<grid, CAND_THREADS, 0, as_stream(stream)>>>(fbv, ld, n_words, rows, width, grp_first, grp_size,
                                                                      cand_off, work_groups, work_off, n_work,
-                                                                     chunk_base, cls, out_counts, min_count, surv_bits);
+                                                                     chunk_base, cls, out_counts, min_count, surv_bits,
+                                                                     occ, occ_ld);
     ETM_LAUNCHED("count_cands");
     return ETM_OK;
 }

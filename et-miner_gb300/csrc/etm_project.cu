@@ -36,11 +36,26 @@ __device__ inline uint64_t prefix_word(const uint64_t* __restrict__ fbv, int64_t
     return p;
 }
 
+// Occupancy word ow of the prefix: bit b set when every prefix column holds a row in tile 64 ow + b (all ones
+// without an occupancy). Words of a tile whose bit is clear have a zero prefix AND and are not read.
+constexpr int64_t OCC_SPAN = 64 * ETM_OCC_TILE_WORDS;  // words per occupancy word
+__device__ inline uint64_t prefix_live(const uint64_t* __restrict__ occ, int64_t occ_ld,
+                                       const int32_t* __restrict__ pref, int plen, int64_t ow) {
+    uint64_t m = ~0ULL;
+    if (occ != nullptr)
+        for (int q = 0; q < plen; q++) m &= __ldg(occ + (int64_t)pref[q] * occ_ld + ow);
+    return m;
+}
+__device__ inline bool tile_live(uint64_t live, int64_t w) {
+    return ((live >> ((w / ETM_OCC_TILE_WORDS) & 63)) & 1ULL) != 0ULL;
+}
+
 __global__ void __launch_bounds__(PT) prefix_counts_kernel(const uint64_t* __restrict__ fbv, int64_t ld,
                                                            int64_t n_words, const int32_t* __restrict__ rows,
                                                            int width, const int64_t* __restrict__ grp_first,
                                                            const int64_t* __restrict__ work_groups,
-                                                           int64_t* __restrict__ out) {
+                                                           int64_t* __restrict__ out,
+                                                           const uint64_t* __restrict__ occ, int64_t occ_ld) {
     __shared__ int32_t pref[64];
     __shared__ unsigned part[PT / 32];
     const int64_t wi = blockIdx.x;
@@ -49,7 +64,13 @@ __global__ void __launch_bounds__(PT) prefix_counts_kernel(const uint64_t* __res
     if (threadIdx.x < plen) pref[threadIdx.x] = rows[first * width + threadIdx.x];
     __syncthreads();
     unsigned s = 0;
-    for (int64_t w = threadIdx.x; w < n_words; w += PT) s += __popcll(prefix_word(fbv, ld, pref, plen, w));
+    for (int64_t w0 = 0; w0 < n_words; w0 += OCC_SPAN) {
+        const uint64_t live = prefix_live(occ, occ_ld, pref, plen, w0 / OCC_SPAN);
+        if (live == 0ULL) continue;  // block-uniform
+        const int64_t w1 = min64(n_words, w0 + OCC_SPAN);
+        for (int64_t w = w0 + threadIdx.x; w < w1; w += PT)
+            if (tile_live(live, w)) s += __popcll(prefix_word(fbv, ld, pref, plen, w));
+    }
     s = __reduce_add_sync(0xffffffffu, s);
     if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
     __syncthreads();
@@ -95,6 +116,7 @@ __global__ void __launch_bounds__(PT) prefix_rows_kernel(const uint64_t* __restr
 // count). Units are (segment, work entry) in segment-major order, so the CTAs running at one time read
 // the same row range of the columns and the column words stay in L2 between groups.
 constexpr int SEG_W = ETM_PROJ_SEG_WORDS;
+static_assert(OCC_SPAN % SEG_W == 0, "a projection segment lies within one occupancy word");
 constexpr int LIST_CAP = 8192;         // prefix rows listed per pass (a segment holds at most 64 SEG_W)
 constexpr int MPI = 4;                 // members gathered per block barrier (independent chains)
 constexpr int NSTAGE = 2 * MPI;        // member segments in shared memory: the current MPI and the next MPI
@@ -155,7 +177,8 @@ __global__ void __launch_bounds__(PT) prefix_segments_kernel(const uint64_t* __r
                                                              int width, const int64_t* __restrict__ grp_first,
                                                              const int64_t* __restrict__ work_groups, int64_t n_seg,
                                                              int64_t* __restrict__ seg_off,
-                                                             int64_t* __restrict__ out_words) {
+                                                             int64_t* __restrict__ out_words,
+                                                             const uint64_t* __restrict__ occ, int64_t occ_ld) {
     __shared__ int32_t pref[64];
     __shared__ unsigned part[P_WARPS];
     const int64_t wi = blockIdx.x;
@@ -168,7 +191,11 @@ __global__ void __launch_bounds__(PT) prefix_segments_kernel(const uint64_t* __r
     for (int64_t s = 0; s < n_seg; s++) {
         const int64_t w1 = min64(n_words, (s + 1) * SEG_W);
         unsigned c = 0;
-        for (int64_t w = s * SEG_W + threadIdx.x; w < w1; w += PT) c += __popcll(prefix_word(fbv, ld, pref, plen, w));
+        // A segment lies within one occupancy word (SEG_W divides OCC_SPAN).
+        const uint64_t live = prefix_live(occ, occ_ld, pref, plen, (s * SEG_W) / OCC_SPAN);
+        if (live != 0ULL)
+            for (int64_t w = s * SEG_W + threadIdx.x; w < w1; w += PT)
+                if (tile_live(live, w)) c += __popcll(prefix_word(fbv, ld, pref, plen, w));
         c = __reduce_add_sync(0xffffffffu, c);
         if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
         __syncthreads();
@@ -411,7 +438,9 @@ __global__ void __launch_bounds__(PT, 2) project_seg_kernel(const uint64_t* __re
         const int64_t* so = seg_off + wi * (n_seg + 1);
         const int64_t stride = cld[wi];
         uint64_t* dst = cbuf + cbase[wi];
-        __syncthreads();  // the previous unit is done with the shared buffers
+        __syncthreads();  // the previous unit is done with the shared buffers (and with next_sh)
+        // A segment without prefix rows adds no words to any member (the last one still zeroes the padding).
+        if (s != n_seg - 1 && so[s + 1] == so[s]) continue;
         if (threadIdx.x < plen) pref[threadIdx.x] = rows[first * width + threadIdx.x];
         __syncthreads();
         int my = 0;
@@ -589,6 +618,8 @@ __global__ void __launch_bounds__(RT, 3) project_rows_kernel(
         uint64_t* dst = cbuf + base;
         __syncthreads();  // the previous unit is done with the shared buffers
         if (m <= 0) continue;
+        // A segment without prefix rows adds no words to any member (the last one still zeroes the padding).
+        if (s != n_seg - 1 && __ldcg(so + s + 1) == __ldcg(so + s)) continue;
         const int32_t* colp = rows + first * width + width - 1;
         const int c_lo = (colp[0] >> 5) & ~3;
         const int nch = ((colp[(m - 1) * width] >> 5) - c_lo + 4) & ~3;  // chunks covered, whole 4-chunk groups
@@ -722,13 +753,15 @@ int proj_status_take(cudaStream_t s, int* out) {
 
 extern "C" int etm_prefix_counts(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
                                  const int64_t* grp_first, const int64_t* work_groups, int64_t n_work,
-                                 int64_t* out_counts, void* stream) {
+                                 int64_t* out_counts, const uint64_t* occ, int64_t occ_ld, void* stream) {
     ETM_REQUIRE(width >= 2 && width <= 64, ETM_EINVAL, "etm_prefix_counts: width %d out of range (2..64)", width);
     ETM_REQUIRE(ld >= n_words, ETM_EINVAL, "etm_prefix_counts: ld < n_words");
     ETM_REQUIRE(n_work < (1LL << 31), ETM_EINVAL, "etm_prefix_counts: too many groups");
+    ETM_REQUIRE(occ == nullptr || occ_ld >= ceil_div<int64_t>(n_words, OCC_SPAN), ETM_EINVAL,
+                "etm_prefix_counts: occ_ld too small for n_words");
     if (n_work <= 0) return ETM_OK;
     prefix_counts_kernel<<<(unsigned)n_work, PT, 0, as_stream(stream)>>>(fbv, ld, n_words, rows, width, grp_first,
-                                                                         work_groups, out_counts);
+                                                                         work_groups, out_counts, occ, occ_ld);
     ETM_LAUNCHED("prefix_counts");
     return ETM_OK;
 }
@@ -748,14 +781,18 @@ extern "C" int etm_prefix_rows(const uint64_t* fbv, int64_t ld, int64_t n_words,
 
 extern "C" int etm_prefix_segments(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows,
                                    int32_t width, const int64_t* grp_first, const int64_t* work_groups,
-                                   int64_t n_work, int64_t* seg_off, int64_t* out_words, void* stream) {
+                                   int64_t n_work, int64_t* seg_off, int64_t* out_words, const uint64_t* occ,
+                                   int64_t occ_ld, void* stream) {
     ETM_REQUIRE(width >= 2 && width <= 64, ETM_EINVAL, "etm_prefix_segments: width %d out of range (2..64)", width);
     ETM_REQUIRE(ld >= n_words && n_words >= 0, ETM_EINVAL, "etm_prefix_segments: bad n_words / ld");
+    ETM_REQUIRE(occ == nullptr || occ_ld >= ceil_div<int64_t>(n_words, OCC_SPAN), ETM_EINVAL,
+                "etm_prefix_segments: occ_ld too small for n_words");
     ETM_REQUIRE(n_work < (1LL << 31), ETM_EINVAL, "etm_prefix_segments: too many groups");
     if (n_work <= 0) return ETM_OK;
     const int64_t n_seg = ceil_div<int64_t>(n_words, SEG_W);
     prefix_segments_kernel<<<(unsigned)n_work, PT, 0, as_stream(stream)>>>(fbv, ld, n_words, rows, width, grp_first,
-                                                                           work_groups, n_seg, seg_off, out_words);
+                                                                           work_groups, n_seg, seg_off, out_words,
+                                                                           occ, occ_ld);
     ETM_LAUNCHED("prefix_segments");
     return ETM_OK;
 }

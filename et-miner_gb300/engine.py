@@ -57,6 +57,7 @@ TC_TILE = 256
 #: Largest group (rows) the tensor-core Gram counts exactly: f32 holds every integer up to 2^24.
 TC_MAX_ROWS = 1 << 24
 PROJ_SEG_WORDS = 1024  # ETM_PROJ_SEG_WORDS: bitvector words per projection segment
+OCC_TILE_WORDS = 32  # ETM_OCC_TILE_WORDS: bitvector words per occupancy tile
 #: Row-wise K=2 crossover: rows' pair increments over pairs x words (the reference's K2_ROWS_MAX_R).
 K2_ROWS_MAX_R = 3.95e-3
 #: Row-wise K=3 crossover: rows' pair increments over K=3 candidates x words, with every candidate in one
@@ -402,9 +403,17 @@ class Engine:
         #: over the prefix rows) instead of gathering every member's segment words (etm_project); the copy is
         #: built once per mine and skipped when it would exceed ``rows_copy_max_bytes``.
         self.proj_rows = bool(proj_rows)
+        #: Row order of the bitvectors that ``apriori(transactions, ...)`` builds for this engine: "lex" (the
+        #: rows sorted by their most frequent columns, and the tile-occupancy skip) or "keep" (input order).
+        self.row_order = "lex"
+        #: Fewer rows than this keep their order: a few tiles per column leave the occupancy little to skip,
+        #: and the keys, sorts and permutation would cost more than they save.
+        self.lex_min_rows = 1 << 18
         self.rows_copy_max_bytes = 32 << 30
         self._xt = None
         self._xt_key = None
+        #: (occupancy, words per column) of the mine's generating columns, when it asked for one.
+        self._occ = None
         #: (level k-2, level k-3 or None, N) of the level being counted, for the deduction bounds.
         self._deep = None
         #: When set, each level's stats count the candidates classified INFER and SKIP (one extra pass per chunk).
@@ -510,10 +519,27 @@ class Engine:
         wg = torch.from_numpy(ids.astype(np.int64)).to(self.device)
         out = self.scratch.get("prefix_counts", len(ids), torch.int64)
         st = self._launch("prefix_counts", len(ids) * (gen.k - 1) * n_words * 8, lambda: self.lib.etm_prefix_counts(
-            _p(fbv), ldp, n_words, _p(gen.rows), gen.k, _p(grp_first), _p(wg), len(ids), _p(out), _stream()))
+            _p(fbv), ldp, n_words, _p(gen.rows), gen.k, _p(grp_first), _p(wg), len(ids), _p(out), *self._occ_args(),
+            _stream()))
         check(st, "etm_prefix_counts")
         self.launches += 1
         return out.cpu().numpy().copy()
+
+    def tile_occupancy(self, fbv: torch.Tensor, ldp: int, n_words: int) -> tuple[torch.Tensor, int]:
+        """(occ int64 [n_cols][occ_ld], occ_ld): per generating column, one bit per tile of ETM_OCC_TILE_WORDS
+        words holding a row of it (etm_tile_occupancy; gpu/kernels/occupancy.py:37-58)."""
+        n_g = int(fbv.shape[0])
+        occ_ld = max(1, -(-(-(-n_words // OCC_TILE_WORDS)) // 64))
+        occ = torch.empty((n_g, occ_ld), dtype=torch.int64, device=self.device)
+        st = self._launch("tile_occupancy", n_g * (n_words + occ_ld) * 8, lambda: self.lib.etm_tile_occupancy(
+            _p(fbv), n_g, n_words, ldp, _p(occ), occ_ld, _stream()))
+        check(st, "etm_tile_occupancy")
+        self.launches += 1
+        return occ, occ_ld
+
+    def _occ_args(self) -> tuple:
+        """The (occ, occ_ld) arguments of the prefix and per-candidate kernels: the mine's tile occupancy, or none."""
+        return (None, 0) if self._occ is None else (_p(self._occ[0]), self._occ[1])
 
     def _rows_copy(self, fbv: torch.Tensor, ldp: int, n_words: int):
         """(xt, ldr): the row-major copy of the mine's generating columns that etm_project_rows reads (word c of
@@ -571,7 +597,7 @@ class Engine:
         st = self._launch("prefix_segments", int(n * (width - 1) * n_words * 8),
                           lambda: self.lib.etm_prefix_segments(_p(fbv), ldp, n_words, _p(gen.rows), width,
                                                                _p(grp_first), _p(wg), n, _p(seg_off), _p(cwords),
-                                                               _stream()))
+                                                               *self._occ_args(), _stream()))
         check(st, "etm_prefix_segments")
         if xt is not None:
             # Algorithmic bytes: the prefix columns' words and the prefix rows' row-major words read once, the
@@ -935,7 +961,8 @@ class Engine:
                         else:
                             fn = lambda: self.lib.etm_count_cands_sel(  # noqa: E731
                                 _p(fbv), ldp, n_words, _p(gen.rows), width, _p(grp_first), _p(grp_size), _p(cand_off),
-                                _p(wg), _p(wo), len(bg), base, _p(cls), mc, _p(counts), _p(bits), _stream())
+                                _p(wg), _p(wo), len(bg), base, _p(cls), mc, _p(counts), _p(bits), *self._occ_args(),
+                                _stream())
                         st = self._launch("count_cands", nbytes, fn)
                     else:
                         # Each group's prefix and suffix columns, once (the same-data minimum). Groups that reach
@@ -1046,7 +1073,8 @@ class Engine:
     def mine(self, bitvecs, n_rows: int, min_support: float, max_length: int | None = None, *,
              prune_equal_support: bool = False, use_generator_pruning: bool = False,
              level_callback=None, n_cols_logical: int | None = None, rows=None, max_ram_gb: float | None = None,
-             max_vram_gb: float | None = None, on_level=None, resume=None, keep_levels: bool = True) -> MineOutput:
+             max_vram_gb: float | None = None, on_level=None, resume=None, keep_levels: bool = True,
+             occupancy: bool = False) -> MineOutput:
         """Mine device bitvectors. ``rows`` = (row_ptr int64, cols int32, host row lengths) on the device,
         the transactions the bitvectors were built from, lets K=2 count row-wise when its rows are short
         against the pair space (the reference's rule, gpu/row_split_chunks.py:124-142).
@@ -1062,11 +1090,16 @@ class Engine:
         ``resume = (k, caller_cols [n, k], counts [n])``: start from a complete emitted level k read back from a
         flush (gpu/row_split.py:546-606): levels 1..k are neither counted nor emitted again; the first resumed
         level has no free flags to infer from, and the deduction bounds wait for levels k-2 and k-3.
+
+        ``occupancy``: build the generating columns' tile occupancy once, and let the prefix and per-candidate
+        kernels skip the tiles where a prefix (or a candidate's) column holds no row. It pays when the rows
+        are in the input layer's lex order, where deep itemsets' rows gather (gpu/row_split.py:397-413).
         """
         ptr, (n_cols, ld), _owner = as_device_bitvecs(bitvecs)
         self._k2_rows = None
         self._rows_input = None
         self._xt, self._xt_key = None, None  # the row-major copy belongs to one mine's generating columns
+        self._occ = None  # so does the tile occupancy
         if n_rows >= 2**31:
             raise ValueError(f"n_transactions={n_rows:,} exceeds int32 max: the count arrays are int32")
         n_words = (n_rows + 63) // 64
@@ -1099,6 +1132,8 @@ class Engine:
             return out
         fbv, ldp = self.gather(ptr, ld, gen_cols, n_words)
         ng = len(gen_cols)
+        if occupancy:
+            self._occ = self.tile_occupancy(fbv, ldp, n_words)
         if rows is not None:
             rp, cl, lens = rows
             pair_work = float((lens.astype(np.float64) * (lens - 1) / 2).sum())
@@ -1159,6 +1194,7 @@ class Engine:
             k += 1
         self._deep = None
         self._xt, self._xt_key = None, None
+        self._occ = None
         return out
 
 

@@ -99,11 +99,11 @@ def dataset_from_transactions(indptr: np.ndarray, items: np.ndarray, device=None
 
     dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
     n_rows = len(indptr) - 1
-    row_ptr, cols, col_items, _ = _frequent_csr_device(np.asarray(indptr, np.int64), np.asarray(items), n_rows, 1, dev)
+    row_ptr, cols, col_items, _, counts = _frequent_csr_device(np.asarray(indptr, np.int64), np.asarray(items), n_rows,
+                                                               1, dev)
     with torch.cuda.device(dev):
         bv = _bitvecs_of_device_csr(row_ptr, cols, len(col_items), n_rows)
-    counts = torch.bincount(cols.long(), minlength=len(col_items)).cpu().numpy().astype(np.int64)
-    return Dataset(bv, col_items.astype(np.int64), n_rows, counts)
+    return Dataset(bv, col_items.astype(np.int64), n_rows, counts.astype(np.int64))
 
 
 class Server:

@@ -69,6 +69,8 @@ extern "C" {
 
 /* Rows of one projection segment: 1024 bitvector words (65,536 transactions). */
 #define ETM_PROJ_SEG_WORDS 1024
+/* Words of one occupancy tile (2,048 transactions); 64 tiles per occupancy word. */
+#define ETM_OCC_TILE_WORDS 32
 
 int etm_version(void);
 /* Message of the last failing call on this thread (empty if none). */
@@ -104,6 +106,36 @@ int etm_popcount_cols(const uint64_t* bv, int64_t n_cols, int64_t n_words, int64
  */
 int etm_gather_cols(const uint64_t* bv, int64_t ld, const int32_t* cols, int32_t n_f, int64_t n_words,
                     uint64_t* out, int64_t out_ld, void* stream);
+
+/*
+ * The lex row order of the device input layer (gpu/input_layer.py:408-430,
+ * the row_order_keys kernel of gpu/kernels/_src/csr_to_bitvec.cu:75-104).
+ *   etm_row_order_keys  per row of a CSR of columns (row_ptr int64 [n_rows+1],
+ *                      cols int32): a row holding the column of rank r
+ *                      (rank_of_col int32 [n_cols], by descending support) sets
+ *                      bit 63 - r of key_hi for r < 64 and bit 127 - r of key_lo
+ *                      for 64 <= r < 128; both int64 [n_rows] are stored with
+ *                      the top bit flipped, so an ascending signed sort by
+ *                      (key_hi, key_lo) is the unsigned order. Columns outside
+ *                      [0, n_cols) are ignored.
+ *   etm_permute_rows   output row p = input row order[p] (order int64 [n_rows],
+ *                      a permutation): its entries go to new_cols from
+ *                      new_row_ptr[p] (the caller's exclusive prefix of the
+ *                      permuted lengths). A row whose source index or either
+ *                      range falls outside [0, n_rows) / [0, nnz) is skipped and
+ *                      sets *status (int32 device word, zeroed here) to 1.
+ *   etm_tile_occupancy per column of bv, one bit per tile of ETM_OCC_TILE_WORDS
+ *                      words (gpu/kernels/occupancy.py:37-58): bit b of
+ *                      occ[c * occ_ld + w] is set when tile 64 w + b (words
+ *                      below n_words) holds a set bit. occ_ld >= ceil(ceil(
+ *                      n_words / 32) / 64); bv 16-byte aligned, ld even.
+ */
+int etm_row_order_keys(const int64_t* row_ptr, const int32_t* cols, int64_t n_rows, const int32_t* rank_of_col,
+                       int64_t n_cols, int64_t* key_hi, int64_t* key_lo, void* stream);
+int etm_permute_rows(const int64_t* row_ptr, const int32_t* cols, int64_t nnz, const int64_t* order, int64_t n_rows,
+                     const int64_t* new_row_ptr, int32_t* new_cols, int32_t* status, void* stream);
+int etm_tile_occupancy(const uint64_t* bv, int64_t n_cols, int64_t n_words, int64_t ld, uint64_t* occ,
+                       int64_t occ_ld, void* stream);
 
 /*
  * Deterministic Bernoulli bitvectors (workload generator; no reference
@@ -242,16 +274,19 @@ int etm_triple_counts_rows(const int64_t* row_ptr, const int32_t* cols, int64_t 
  *                      is zeroed on the stream first (one per concurrent call).
  *   etm_count_tiles_proj  etm_count_tiles over the projected words
  *                      (cwords[wi] words per member; no prefix AND).
+ * occ (etm_prefix_counts, etm_prefix_segments; NULL for none): the tile
+ * occupancy of fbv (etm_tile_occupancy over n_words, occ_ld words per column);
+ * a tile where a prefix column holds no row is not read, its prefix AND is 0.
  */
 int etm_prefix_counts(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
                       const int64_t* grp_first, const int64_t* work_groups, int64_t n_work, int64_t* out_counts,
-                      void* stream);
+                      const uint64_t* occ, int64_t occ_ld, void* stream);
 int etm_prefix_rows(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
                     const int64_t* grp_first, const int64_t* work_groups, int64_t n_work, const int64_t* row_off,
                     int32_t* out_rows, void* stream);
 int etm_prefix_segments(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
                         const int64_t* grp_first, const int64_t* work_groups, int64_t n_work, int64_t* seg_off,
-                        int64_t* out_words, void* stream);
+                        int64_t* out_words, const uint64_t* occ, int64_t occ_ld, void* stream);
 int etm_project(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
                 const int64_t* grp_first, const int32_t* grp_size, const int64_t* work_groups, int64_t n_work,
                 const int64_t* seg_off, const int64_t* cbase, const int64_t* cld, uint64_t* cbuf,
@@ -412,7 +447,10 @@ int etm_count_tiles_split(const uint64_t* fbv, int64_t ld, int64_t n_words, cons
  * (deep2: rows [deep2_n][k-2] sorted, counts) and, for k > 3, k-3 (deep3),
  * with n_transactions the count of the empty set at k = 3. Arguments otherwise as
  * in the dense forms (etm_count_tiles with the popcount method,
- * etm_count_cands, etm_count_tiles_proj, etm_classify).
+ * etm_count_cands, etm_count_tiles_proj, etm_classify). etm_count_cands_sel
+ * takes the tile occupancy of fbv (occ, occ_ld; NULL for none, see
+ * etm_tile_occupancy): a tile where one of the candidate's columns holds no
+ * row is not read.
  */
 int etm_count_tiles_sel(const uint64_t* fbv, int64_t ld, int64_t n_words, const int32_t* rows, int32_t width,
                         const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
@@ -423,7 +461,7 @@ int etm_count_cands_sel(const uint64_t* fbv, int64_t ld, int64_t n_words, const 
                         const int64_t* grp_first, const int32_t* grp_size, const int64_t* cand_off,
                         const int64_t* work_groups, const int64_t* work_off, int64_t n_work, int64_t chunk_base,
                         const uint8_t* cls, int32_t min_count, int32_t* out_counts, uint32_t* surv_bits,
-                        void* stream);
+                        const uint64_t* occ, int64_t occ_ld, void* stream);
 int etm_count_tiles_proj_sel(const uint64_t* cbuf, const int64_t* cbase, const int64_t* cwords, const int64_t* cld,
                              const int32_t* grp_size, const int64_t* cand_off, const int64_t* work_groups,
                              const int64_t* work_off, int64_t n_work, int64_t chunk_base, const uint8_t* cls,

@@ -38,6 +38,24 @@ def test_bound_signatures_cover_header(pkg):
     assert set(declared_symbols()) <= set(lib_mod.SIGNATURES), set(declared_symbols()) - set(lib_mod.SIGNATURES)
 
 
+def test_bound_argument_counts_match_header(pkg):
+    """Every binding passes as many arguments as its declaration takes (a missing one would shift the rest)."""
+    from importlib import import_module
+
+    lib_mod = import_module(pkg.__name__ + "._lib")
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    decls = re.findall(r"\b(?:int|void|const char\s*\*)\s+(etm_[a-z0-9_]+)\s*\(([^;]*?)\)\s*;", text)
+    assert len(decls) >= len(declared_symbols()) - 1
+    wrong = []
+    for name, args in decls:
+        args = args.strip()
+        n = 0 if args in ("", "void") else args.count(",") + 1
+        bound = lib_mod.SIGNATURES[name][1]
+        if bound is not None and len(bound) != n:
+            wrong.append((name, n, len(bound)))
+    assert not wrong, wrong
+
+
 def test_loads_and_reports_version(pkg):
     lib = pkg.load_library()
     assert lib.etm_version() >= 1

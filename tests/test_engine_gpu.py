@@ -28,6 +28,12 @@ def _rows_engine(e, k3=False):
     return e
 
 
+def _lex_engine(e):
+    """An engine whose transactions always take the lex row order (and the tile-occupancy skip)."""
+    e.lex_min_rows = 0
+    return e
+
+
 @pytest.fixture(scope="module")
 def engines(pkg):
     from importlib import import_module
@@ -48,6 +54,8 @@ def engines(pkg):
         "rows_dense": _rows_engine(eng.Engine(fused=False), k3=True),
         "proj_cols": eng.Engine(form="batched", small_group=2, proj_density=1.01, proj_bytes=1 << 14, proj_rows=False),
         "popcount_rows": eng.Engine(method="popcount", small_group=2, proj_density=1.01),
+        "lex": _lex_engine(eng.Engine()),
+        "lex_proj": _lex_engine(eng.Engine(form="batched", small_group=2, proj_density=1.01, proj_bytes=1 << 14)),
     }
 
 
@@ -67,7 +75,7 @@ def test_transactions_match_golden(pkg, golden_cases, engines, name):
 
 
 @pytest.mark.parametrize("form", ["plain", "tiny", "proj", "noproj", "popcount", "tuned", "rows", "rows3", "dense",
-                                  "dense_tiny", "rows_dense", "proj_cols", "popcount_rows"])
+                                  "dense_tiny", "rows_dense", "proj_cols", "popcount_rows", "lex", "lex_proj"])
 @pytest.mark.parametrize("name", ["implication_plain", "implication_prune", "implication_infer", "plain_small_plain",
                                   "deep_sparse_small", "dense_k2_small", "word_tail_65"])
 def test_forms_match_golden(pkg, golden_cases, engines, name, form):

@@ -25,12 +25,13 @@ def test_device_frequent_csr_matches_host(pkg, wide, mc):
     else:
         flat = (ids * 1_000_003 - 7_000_000).astype(np.int64)  # negative ids too
     rp_h, cols_h, items_h = api._frequent_csr(indptr, flat, n_rows, mc)
-    rp_d, cols_d, items_d, row_len = api._frequent_csr_device(indptr, flat, n_rows, mc, "cpu")
+    rp_d, cols_d, items_d, row_len, support = api._frequent_csr_device(indptr, flat, n_rows, mc, "cpu")
     assert items_d.dtype == items_h.dtype
     assert np.array_equal(items_d, items_h)
     assert np.array_equal(rp_d.numpy(), rp_h)
     assert np.array_equal(cols_d.numpy(), cols_h)
     assert np.array_equal(row_len, np.diff(rp_h))
+    assert np.array_equal(support, np.bincount(cols_h, minlength=len(items_h)))
 
 
 @pytest.mark.parametrize("kw,exc,match", [

@@ -1,0 +1,199 @@
+"""GPU parity of the input layer's lex row order and the tile-occupancy skip.
+
+The row order keys, the row permutation and the tile occupancy are checked word for word against host
+restatements; mining with the occupancy skip, and through the transactions route in lex order, must give
+exactly the itemsets and counts of the same mine without them.
+"""
+
+from __future__ import annotations
+
+from importlib import import_module
+
+import numpy as np
+import pytest
+
+from tests.helpers import table_of
+
+pytestmark = pytest.mark.gpu
+
+TOP = np.uint64(1 << 63)
+
+
+def _stream():
+    import torch
+
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _host_keys(rp: np.ndarray, cols: np.ndarray, rank: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """The lex order keys (gpu/kernels/_src/csr_to_bitvec.cu:75-104) as unsigned values."""
+    n = len(rp) - 1
+    hi = np.zeros(n, np.uint64)
+    lo = np.zeros(n, np.uint64)
+    for r in range(n):
+        for c in cols[rp[r]:rp[r + 1]]:
+            k = int(rank[c])
+            if k < 64:
+                hi[r] |= np.uint64(1) << np.uint64(63 - k)
+            elif k < 128:
+                lo[r] |= np.uint64(1) << np.uint64(127 - k)
+    return hi, lo
+
+
+def _random_csr(rng, n_rows: int, n_cols: int, max_len: int):
+    lens = rng.integers(0, max_len + 1, n_rows)
+    lens[::29] = 0
+    rp = np.zeros(n_rows + 1, np.int64)
+    np.cumsum(lens, out=rp[1:])
+    cols = np.concatenate([np.sort(rng.choice(n_cols, size=int(k), replace=False)) for k in lens]).astype(np.int32) \
+        if lens.sum() else np.zeros(0, np.int32)
+    return rp, cols
+
+
+@pytest.mark.parametrize("n_cols", [40, 200])
+def test_row_order_keys_and_permutation(pkg, n_cols):
+    import torch
+
+    api = import_module(pkg.__name__ + ".api")
+    lib = pkg.load_library()
+    rng = np.random.default_rng(n_cols)
+    n_rows = 3_001
+    rp, cols = _random_csr(rng, n_rows, n_cols, 30)
+    support = np.bincount(cols, minlength=n_cols)
+    rank = np.empty(n_cols, np.int32)
+    rank[np.argsort(-support, kind="stable")] = np.arange(n_cols, dtype=np.int32)
+    rp_d = torch.from_numpy(rp).cuda()
+    cols_d = torch.from_numpy(cols).cuda()
+    key_hi = torch.empty(n_rows, dtype=torch.int64, device="cuda")
+    key_lo = torch.empty(n_rows, dtype=torch.int64, device="cuda")
+    st = lib.etm_row_order_keys(rp_d.data_ptr(), cols_d.data_ptr(), n_rows, torch.from_numpy(rank).cuda().data_ptr(),
+                                n_cols, key_hi.data_ptr(), key_lo.data_ptr(), _stream())
+    assert st == 0, lib.etm_last_error()
+    hi, lo = _host_keys(rp, cols, rank)
+    assert np.array_equal(key_hi.cpu().numpy().view(np.uint64) ^ TOP, hi)
+    assert np.array_equal(key_lo.cpu().numpy().view(np.uint64) ^ TOP, lo)
+
+    new_rp, new_cols, new_len = api._lex_order(rp_d, cols_d, support)
+    order = np.lexsort((lo, hi))  # stable: by (hi, lo) ascending, ties in input order
+    want_len = np.diff(rp)[order]
+    assert np.array_equal(new_len, want_len)
+    assert np.array_equal(new_rp.cpu().numpy()[1:], np.cumsum(want_len))
+    want_cols = np.concatenate([cols[rp[r]:rp[r + 1]] for r in order])
+    assert np.array_equal(new_cols.cpu().numpy(), want_cols)
+
+
+def test_permute_rows_refuses_a_bad_order(pkg):
+    """An order entry outside [0, n_rows) is skipped on the device and reported, not followed."""
+    import torch
+
+    lib = pkg.load_library()
+    rp = torch.tensor([0, 2, 3, 5], dtype=torch.int64, device="cuda")
+    cols = torch.tensor([1, 4, 2, 0, 3], dtype=torch.int32, device="cuda")
+    order = torch.tensor([2, 7, 0], dtype=torch.int64, device="cuda")
+    new_rp = torch.tensor([0, 2, 3, 5], dtype=torch.int64, device="cuda")
+    out = torch.full((5,), -1, dtype=torch.int32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = lib.etm_permute_rows(rp.data_ptr(), cols.data_ptr(), 5, order.data_ptr(), 3, new_rp.data_ptr(),
+                              out.data_ptr(), status.data_ptr(), _stream())
+    assert st == 0, lib.etm_last_error()
+    assert int(status.item()) == 1
+    assert out.cpu().tolist() == [0, 3, -1, 1, 4]
+
+
+@pytest.mark.parametrize("n_words", [1, 31, 32, 33, 2_047, 2_048, 2_049, 5_000])
+def test_tile_occupancy_matches_host(pkg, n_words):
+    import torch
+
+    lib = pkg.load_library()
+    rng = np.random.default_rng(n_words)
+    n_cols = 7
+    ld = n_words + (n_words % 2) + 2
+    bv = np.zeros((n_cols, ld), np.uint64)
+    for c in range(n_cols):
+        # A few words set per column, some columns empty, garbage past n_words that must be ignored.
+        if c % 3 == 2:
+            continue
+        at = rng.choice(n_words, size=max(1, n_words // (50 * (c + 1))), replace=False)
+        bv[c, at] = rng.integers(1, 2**63, len(at)).astype(np.uint64)
+    bv[:, n_words:] = np.uint64(0xFFFF)
+    tiles = -(-n_words // 32)
+    occ_ld = -(-tiles // 64) + 1
+    occ = torch.full((n_cols, occ_ld), -1, dtype=torch.int64, device="cuda")
+    d = torch.from_numpy(bv.view(np.int64)).cuda()
+    st = lib.etm_tile_occupancy(d.data_ptr(), n_cols, n_words, ld, occ.data_ptr(), occ_ld, _stream())
+    assert st == 0, lib.etm_last_error()
+    want = np.zeros((n_cols, occ_ld), np.uint64)
+    for c in range(n_cols):
+        for t in range(64 * occ_ld):
+            lo, hi = 32 * t, min(n_words, 32 * t + 32)
+            if lo < hi and (bv[c, lo:hi] != 0).any():
+                want[c, t // 64] |= np.uint64(1) << np.uint64(t % 64)
+    assert np.array_equal(occ.cpu().numpy().view(np.uint64), want)
+    assert lib.etm_tile_occupancy(d.data_ptr(), n_cols, n_words, ld, occ.data_ptr(), 0, _stream()) == 1
+
+
+def _topic_bitvecs(n_rows: int, seed: int):
+    """Rows in blocks of 4,096, block b on topic b % 10: the topic's 12 items at 0.5 each in its rows, one wide
+    topic (40 items at 0.45) on every fourth block, and 4 items at 0.05 everywhere. Most 32-word tiles hold no
+    row of a topic item, so the occupancy skips most of them."""
+    rng = np.random.default_rng(seed)
+    n_items = 10 * 12 + 40 + 4
+    dense = np.zeros((n_rows, n_items), bool)
+    for b0 in range(0, n_rows, 4096):
+        b = b0 // 4096
+        r = slice(b0, min(n_rows, b0 + 4096))
+        n = r.stop - r.start
+        t = b % 10
+        dense[r, 12 * t:12 * t + 12] = rng.random((n, 12)) < 0.5
+        if b % 4 == 0:
+            dense[r, 120:160] = rng.random((n, 40)) < 0.45
+    dense[:, 160:] = rng.random((n_rows, 4)) < 0.05
+    n_words = -(-n_rows // 64)
+    bits = np.packbits(dense.T, axis=1, bitorder="little")
+    pad = np.zeros((n_items, n_words * 8), np.uint8)
+    pad[:, :bits.shape[1]] = bits
+    return pad.view(np.uint64), n_items
+
+
+@pytest.mark.parametrize("form", ["batched", "popcount", "plain", "proj", "proj_cols"])
+def test_occupancy_skip_leaves_counts_unchanged(pkg, form):
+    import torch
+
+    engm = import_module(pkg.__name__ + ".engine")
+    kw = {"batched": {}, "popcount": dict(method="popcount"), "plain": dict(form="plain"),
+          "proj": dict(small_group=2, proj_density=1.01, proj_bytes=1 << 16),
+          "proj_cols": dict(small_group=2, proj_density=1.01, proj_bytes=1 << 16, proj_rows=False)}[form]
+    bv, n_items = _topic_bitvecs(150_000, 3)
+    dev = torch.from_numpy(bv.view(np.int64)).cuda().view(torch.uint64)
+    res = []
+    for occ in (False, True):
+        eng = engm.Engine(**kw)
+        eng.profile_kernels = True
+        out = eng.mine(dev, 150_000, 0.003, 4, occupancy=occ)
+        res.append(out.host_levels())
+        if occ:
+            assert "tile_occupancy" in eng.kernel_report()
+    a, b = res
+    assert len(a) == len(b) >= 3
+    for (ra, ca), (rb, cb) in zip(a, b):
+        assert np.array_equal(ra, rb) and np.array_equal(ca, cb)
+
+
+def test_transactions_in_lex_order_match_input_order(pkg):
+    """apriori(transactions): the lex row order with the occupancy skip against the rows in input order."""
+    engm = import_module(pkg.__name__ + ".engine")
+    bv, n_items = _topic_bitvecs(60_000, 11)
+    dense = np.unpackbits(bv.view(np.uint8), axis=1, bitorder="little")[:, :60_000].T.astype(bool)
+    rows_i, cols_i = np.nonzero(dense)
+    indptr = np.zeros(60_001, np.int64)
+    np.cumsum(np.bincount(rows_i, minlength=60_000), out=indptr[1:])
+    items = (cols_i * 7 + 3).astype(np.int64)  # ids that are not the columns
+    got = []
+    for order in ("lex", "keep"):
+        eng = engm.Engine()
+        eng.row_order, eng.lex_min_rows = order, 0
+        df = pkg.apriori(table_of(indptr, items, 60_000), min_support=0.004, max_length=4, use_gpu=True, engine=eng,
+                         warn_complexity=False)
+        got.append(pkg.result_pairs(df, 60_000))
+    assert got[0] == got[1]
+    assert max(len(s) for s, _ in got[0]) == 4

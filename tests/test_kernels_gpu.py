@@ -427,7 +427,8 @@ def test_segmented_projection(pkg, lib, n_words, width, n_cols, blk, form):
     seg_off = torch.full((len(wg) * (n_seg + 1),), -7, dtype=torch.int64, device="cuda")
     out_words = torch.full((len(wg),), -7, dtype=torch.int64, device="cuda")
     st = lib.etm_prefix_segments(d_fbv.data_ptr(), ld, n_words, d_rows.data_ptr(), width, d_first.data_ptr(),
-                                 d_wg.data_ptr(), len(wg), seg_off.data_ptr(), out_words.data_ptr(), _stream())
+                                 d_wg.data_ptr(), len(wg), seg_off.data_ptr(), out_words.data_ptr(), None, 0,
+                                 _stream())
     assert st == 0, lib.etm_last_error()
     cbuf = torch.full((int(cb[-1]),), -1, dtype=torch.int64, device="cuda")
     # Alternate the dynamic (work counter) and round-robin unit orders across the cases.
