@@ -30,7 +30,7 @@ def _rows_engine(e, k3=False):
 
 def _lex_engine(e):
     """An engine whose transactions always take the lex row order (and the tile-occupancy skip)."""
-    e.lex_min_rows = 0
+    e.row_order, e.lex_min_rows = "lex", 0
     return e
 
 
