@@ -94,6 +94,10 @@ SIGNATURES: dict[str, tuple] = {
     "etm_row_order_keys": (ctypes.c_int, [_P, _P, _I64, _P, _I64, _P, _P, _P]),
     "etm_permute_rows": (ctypes.c_int, [_P, _P, _I64, _P, _I64, _P, _P, _P, _P]),
     "etm_tile_occupancy": (ctypes.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P]),
+    "etm_item_codes": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _I64, _P, _P, _P, _P, _P]),
+    "etm_code_histogram": (ctypes.c_int, [_P, _I64, _I64, _P, _P]),
+    "etm_bitmap_values": (ctypes.c_int, [_P, _I64, _P, _I64, _P, _P]),
+    "etm_kept_lengths": (ctypes.c_int, [_P, _P, _I64, _P, _I64, _P, _P]),
     "etm_synth_bernoulli": (ctypes.c_int, [_P, _I32, _I64, _U64, _P, _I64, _P]),
     "etm_synth_patterns": (ctypes.c_int, [_P, _I32, _P, _I32, _P, _P, _I32, _U64, _I32, _I64, _U64, _P, _I64, _P]),
     "etm_level_groups": (ctypes.c_int, [_P, _I64, _I32, _P, _P, _P, _P, _P, _I64, _P]),

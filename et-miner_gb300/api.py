@@ -292,6 +292,89 @@ def _frequent_csr_device(indptr: np.ndarray, flat: np.ndarray, n_rows: int, mc: 
             counts[keep].cpu().numpy())
 
 
+@dataclass
+class _CodedInput:
+    """The transactions coded on the device (``_coded_csr_device``)."""
+
+    row_ptr: Any      # int64 [n_rows + 1], device
+    codes: Any        # int32 [nnz], device: each entry's rank among the distinct ids
+    col_of: Any       # int32 [n_distinct], device: the column of each code, -1 for an infrequent id
+    items: np.ndarray  # the columns' ids, ascending
+    row_len: np.ndarray  # each row's entries in the columns
+    support: np.ndarray  # the columns' supports
+    code_support: np.ndarray  # every code's support (the lex order ranks codes)
+
+
+def _coded_csr_device(indptr: np.ndarray, flat: np.ndarray, n_rows: int, mc: int, device) -> _CodedInput | None:
+    """The transactions coded on the device without a sort: a presence bitmap over the id span gives every id
+    its rank among the distinct ids (etm_item_codes), the rows' occurrences of each rank are its support
+    (etm_code_histogram), the ids with support >= mc are the columns in ascending id order, and the
+    bitvectors and the row-wise kernels read the codes through the code -> column table. The same columns,
+    supports and rows as ``_frequent_csr_device`` (the device input layer, gpu/input_layer.py:396-466).
+
+    None (take ``_frequent_csr_device``) for ids that are not 64-bit signed integers within a span of
+    ETM_CODE_SPAN_MAX, or when a row is not canonical (its ids unsorted or repeated), where the occurrences
+    would not be supports.
+    """
+    import torch
+
+    from ._lib import check, load_library
+
+    nnz = len(flat)
+    if nnz == 0 or n_rows == 0 or flat.dtype == np.uint64 or not np.issubdtype(flat.dtype, np.integer):
+        return None
+    lib = load_library()
+    stream = torch.cuda.current_stream(device).cuda_stream
+    vals = torch.from_numpy(np.ascontiguousarray(flat).astype(np.int64, copy=False)).to(device)
+    lo_hi = torch.stack(torch.aminmax(vals)).cpu().numpy()
+    lo, span = int(lo_hi[0]), int(lo_hi[1]) - int(lo_hi[0]) + 1
+    if span > CODE_SPAN_MAX:
+        return None
+    n_w = -(-span // 32)
+    row_ptr = torch.from_numpy(np.ascontiguousarray(indptr, dtype=np.int64)).to(device)
+    bitmap = torch.empty(n_w, dtype=torch.int32, device=device)
+    word_rank = torch.empty(n_w + 1, dtype=torch.int64, device=device)
+    codes = torch.empty(nnz, dtype=torch.int32, device=device)
+    status = torch.empty(2, dtype=torch.int32, device=device)
+    check(lib.etm_item_codes(row_ptr.data_ptr(), vals.data_ptr(), nnz, n_rows, lo, span, bitmap.data_ptr(),
+                             word_rank.data_ptr(), codes.data_ptr(), status.data_ptr(), stream), "etm_item_codes")
+    st = status.cpu().numpy()
+    n_distinct = int(word_rank[n_w].item())
+    if st[0] != 0 or n_distinct < 1:
+        raise RuntimeError("etm_item_codes: an id fell outside the span of the ids")
+    if st[1] != 0:
+        return None
+    counts = torch.empty(n_distinct, dtype=torch.int64, device=device)
+    check(lib.etm_code_histogram(codes.data_ptr(), nnz, n_distinct, counts.data_ptr(), stream), "etm_code_histogram")
+    ids = torch.empty(n_distinct, dtype=torch.int64, device=device)
+    check(lib.etm_bitmap_values(bitmap.data_ptr(), span, word_rank.data_ptr(), lo, ids.data_ptr(), stream),
+          "etm_bitmap_values")
+    keep = counts >= max(1, mc)
+    col_of = torch.cumsum(keep.to(torch.int32), 0, dtype=torch.int32) - 1
+    col_of[~keep] = -1
+    code_support = counts.cpu().numpy()
+    keep_h = code_support >= max(1, mc)
+    return _CodedInput(row_ptr, codes, col_of, ids.cpu().numpy()[keep_h], _kept_lengths(row_ptr, codes, col_of),
+                       code_support[keep_h], code_support)
+
+
+def _kept_lengths(row_ptr, codes, col_of) -> np.ndarray:
+    """Each row's entries whose code maps to a column (etm_kept_lengths), on the host."""
+    import torch
+
+    from ._lib import check, load_library
+
+    n_rows = int(row_ptr.numel()) - 1
+    out = torch.empty(max(1, n_rows), dtype=torch.int64, device=row_ptr.device)
+    check(load_library().etm_kept_lengths(row_ptr.data_ptr(), codes.data_ptr(), n_rows, col_of.data_ptr(),
+                                          col_of.numel(), out.data_ptr(),
+                                          torch.cuda.current_stream(row_ptr.device).cuda_stream), "etm_kept_lengths")
+    return out[:n_rows].cpu().numpy()
+
+
+#: Widest id span coded through the presence bitmap (ETM_CODE_SPAN_MAX).
+CODE_SPAN_MAX = 1 << 26
+
 #: Device bytes per row the lex row order holds at its peak (two int64 keys, the sort's keys, indices and
 #: buffers, the permuted lengths and offsets), plus 4 per entry for the permuted columns; without them free the
 #: rows keep their order (gpu/input_layer.py:56-58, 500-529).
@@ -350,8 +433,9 @@ def _lex_order(row_ptr, cols, support: np.ndarray):
         return None
 
 
-def _bitvecs_of_device_csr(row_ptr, cols, n_cols: int, n_rows: int):
-    """Column bitvectors [n_cols, ceil(N/64)] (torch int64) from a device CSR (etm_build_bitvecs)."""
+def _bitvecs_of_device_csr(row_ptr, cols, n_cols: int, n_rows: int, lut=None):
+    """Column bitvectors [n_cols, ceil(N/64)] (torch int64) from a device CSR (etm_build_bitvecs); with ``lut``
+    (int32, -1 for none) the entries are codes and ``lut`` their columns."""
     import torch
 
     from ._lib import check, load_library
@@ -360,8 +444,10 @@ def _bitvecs_of_device_csr(row_ptr, cols, n_cols: int, n_rows: int):
     ld = max(1, (n_rows + 63) // 64)
     bv = torch.empty((max(n_cols, 1), ld), dtype=torch.int64, device=row_ptr.device)
     ids = cols if cols.numel() else torch.zeros(1, dtype=torch.int32, device=row_ptr.device)
-    check(lib.etm_build_bitvecs(row_ptr.data_ptr(), ids.data_ptr(), cols.numel(), None, 0, n_rows, n_cols, ld,
-                                bv.data_ptr(), torch.cuda.current_stream().cuda_stream), "etm_build_bitvecs")
+    check(lib.etm_build_bitvecs(row_ptr.data_ptr(), ids.data_ptr(), cols.numel(),
+                                None if lut is None else lut.data_ptr(), 0 if lut is None else lut.numel(), n_rows,
+                                n_cols, ld, bv.data_ptr(), torch.cuda.current_stream().cuda_stream),
+          "etm_build_bitvecs")
     return bv[:n_cols]
 
 
@@ -717,16 +803,26 @@ def apriori(
         raise ValueError(f"n_transactions={n_rows:,} exceeds int32 max")
     wide = np.dtype(kind) == np.uint64
     mc = min_count(min_support, n_rows)
-    row_ptr, cols, items, row_len, support = _frequent_csr_device(indptr, flat, n_rows, mc, eng.device)
+    coded = _coded_csr_device(indptr, flat, n_rows, mc, eng.device)
+    if coded is not None:
+        # Entries hold codes; col_of maps them to the columns.
+        row_ptr, cols, items, row_len, col_of = coded.row_ptr, coded.codes, coded.items, coded.row_len, coded.col_of
+        rank_support = np.where(coded.code_support >= max(1, mc), coded.code_support, -1)
+    else:
+        row_ptr, cols, items, row_len, rank_support = _frequent_csr_device(indptr, flat, n_rows, mc, eng.device)
+        col_of = None
     if len(items) == 0:
         df = _frame([], max(1, n_rows), wide)
         return (df, session) if profile else df
     # The lex row order, and with it the tile-occupancy skip (core/apriori.py:627-640, gpu/row_split.py:397-413).
-    lex = _lex_order(row_ptr, cols, support) if eng.row_order == "lex" and n_rows >= eng.lex_min_rows else None
+    lex = (_lex_order(row_ptr, cols, rank_support) if eng.row_order == "lex" and n_rows >= eng.lex_min_rows
+           else None)
     if lex is not None:
         row_ptr, cols, row_len = lex
-    bv = _bitvecs_of_device_csr(row_ptr, cols, len(items), n_rows)
-    rows = (row_ptr, cols, row_len)
+        if col_of is not None:
+            row_len = _kept_lengths(row_ptr, cols, col_of)  # the rows' entries in the columns, in the new order
+    bv = _bitvecs_of_device_csr(row_ptr, cols, len(items), n_rows, col_of)
+    rows = (row_ptr, cols, row_len) if col_of is None else (row_ptr, cols, row_len, col_of)
     max_tx = int(np.diff(indptr).max()) if n_rows else 0
     eff = min(max_length, max_tx) if max_length else max_tx
     col_items = items.astype(np.uint64 if wide else np.int64)

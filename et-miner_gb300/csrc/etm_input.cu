@@ -103,6 +103,136 @@ __global__ void __launch_bounds__(IN_THREADS) tile_occupancy_kernel(const uint64
     }
 }
 
+// ---- item coding of a transaction CSR: ids to ranks among the distinct ids, without sorting ----
+
+// Bit (id - lo) of the bitmap for every entry with lo <= id < lo + span; an id outside sets *bad. A bit already
+// set is not OR-ed again, so a frequent id costs a read, not an atomic.
+__global__ void __launch_bounds__(IN_THREADS) id_presence_kernel(const int64_t* __restrict__ ids, int64_t nnz,
+                                                                 int64_t lo, int64_t span, uint32_t* bitmap,
+                                                                 int* bad) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += stride) {
+        const uint64_t v = (uint64_t)ids[e] - (uint64_t)lo;
+        if (v >= (uint64_t)span) {
+            atomicExch(bad, 1);
+            continue;
+        }
+        const unsigned bit = 1u << (v & 31);
+        unsigned* w = bitmap + (v >> 5);
+        if ((__ldcg(w) & bit) == 0u) atomicOr(w, bit);
+    }
+}
+
+// One block: word_rank[w] = set bits in words [0, w) of the bitmap, word_rank[n] = the distinct ids.
+__global__ void __launch_bounds__(1024) bitmap_rank_kernel(const uint32_t* __restrict__ bitmap, int64_t n,
+                                                           int64_t* __restrict__ word_rank) {
+    int64_t carry = 0;  // the same in every thread
+    for (int64_t w0 = 0; w0 < n; w0 += blockDim.x) {
+        const int64_t w = w0 + threadIdx.x;
+        int64_t total;
+        const int64_t ex = block_exclusive_scan(w < n ? __popc(bitmap[w]) : 0, &total);
+        if (w < n) word_rank[w] = carry + ex;
+        carry += total;
+    }
+    if (threadIdx.x == 0) word_rank[n] = carry;
+}
+
+// One warp per row: each entry's code, the rank of its id among the distinct ids (word_rank[w] plus the set
+// bits below it in word w), and the canonical check: a row whose codes do not strictly ascend (an unsorted
+// row, or a repeated id) sets *noncanonical.
+__global__ void __launch_bounds__(IN_THREADS) code_rows_kernel(const int64_t* __restrict__ row_ptr,
+                                                               const int64_t* __restrict__ ids, int64_t n_rows,
+                                                               int64_t lo, int64_t span,
+                                                               const uint32_t* __restrict__ bitmap,
+                                                               const int64_t* __restrict__ word_rank,
+                                                               int32_t* __restrict__ codes, int* noncanonical) {
+    const int lane = threadIdx.x & 31;
+    const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_rows; r += n_warps) {
+        const int64_t e0 = row_ptr[r], e1 = row_ptr[r + 1];
+        int64_t carry = -1;  // the code of the previous (full) chunk's last entry
+        bool bad = false;
+        for (int64_t base = e0; base < e1; base += 32) {
+            const int64_t e = base + lane;
+            int64_t code = -1;
+            if (e < e1) {
+                const uint64_t v = (uint64_t)ids[e] - (uint64_t)lo;
+                if (v < (uint64_t)span) {
+                    const uint32_t word = bitmap[v >> 5];
+                    code = word_rank[v >> 5] + __popc(word & ((1u << (v & 31)) - 1u));
+                }
+                codes[e] = (int32_t)code;
+            }
+            int64_t prev = __shfl_up_sync(0xffffffffu, code, 1);
+            if (lane == 0) prev = carry;
+            if (e < e1 && (code < 0 || (e > e0 && code <= prev))) bad = true;
+            carry = __shfl_sync(0xffffffffu, code, 31);
+        }
+        if (__any_sync(0xffffffffu, bad) && lane == 0) atomicExch(noncanonical, 1);
+    }
+}
+
+constexpr int HIST_SMEM_BINS = 12288;  // 48 KB of block-private counters
+
+// Occurrences of each code in [0, n_bins) (others ignored): block-private shared counters when the bins fit,
+// added to the global counts once per non-zero bin; global atomics otherwise.
+template <bool SMEM>
+__global__ void __launch_bounds__(IN_THREADS) code_histogram_kernel(const int32_t* __restrict__ codes, int64_t nnz,
+                                                                    int64_t n_bins,
+                                                                    unsigned long long* __restrict__ counts) {
+    extern __shared__ uint32_t hist[];
+    if (SMEM) {
+        for (int64_t i = threadIdx.x; i < n_bins; i += blockDim.x) hist[i] = 0u;
+        __syncthreads();
+    }
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += stride) {
+        const int32_t c = codes[e];
+        if (c < 0 || c >= n_bins) continue;
+        if (SMEM) atomicAdd(hist + c, 1u);
+        else atomicAdd(counts + c, 1ULL);
+    }
+    if (SMEM) {
+        __syncthreads();
+        for (int64_t i = threadIdx.x; i < n_bins; i += blockDim.x)
+            if (hist[i] != 0u) atomicAdd(counts + i, (unsigned long long)hist[i]);
+    }
+}
+
+// The distinct ids in ascending order: lo + 32 w + b for every set bit b of word w, at out[word_rank[w]] on.
+__global__ void __launch_bounds__(IN_THREADS) bitmap_values_kernel(const uint32_t* __restrict__ bitmap, int64_t n,
+                                                                   const int64_t* __restrict__ word_rank, int64_t lo,
+                                                                   int64_t* __restrict__ out) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += stride) {
+        uint32_t x = bitmap[w];
+        int64_t at = word_rank[w];
+        while (x) {
+            const int b = __ffs(x) - 1;
+            out[at++] = lo + 32 * w + b;
+            x &= x - 1u;
+        }
+    }
+}
+
+// One warp per row: its entries whose code maps to a column (0 <= code < lut_size and lut[code] >= 0).
+__global__ void __launch_bounds__(IN_THREADS) kept_lengths_kernel(const int64_t* __restrict__ row_ptr,
+                                                                  const int32_t* __restrict__ codes, int64_t n_rows,
+                                                                  const int32_t* __restrict__ lut, int64_t lut_size,
+                                                                  int64_t* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_rows; r += n_warps) {
+        unsigned n = 0;
+        for (int64_t e = row_ptr[r] + lane; e < row_ptr[r + 1]; e += 32) {
+            const int32_t c = codes[e];
+            n += (c >= 0 && c < lut_size && lut[c] >= 0) ? 1u : 0u;
+        }
+        n = __reduce_add_sync(0xffffffffu, n);
+        if (lane == 0) out[r] = n;
+    }
+}
+
 int in_grid(int64_t units_of_warps) {
     const int64_t cap = (int64_t)max(1, sm_count()) * 8;
     return (int)max64(1, min64(cap, ceil_div<int64_t>(units_of_warps, IN_THREADS / 32)));
@@ -147,5 +277,68 @@ extern "C" int etm_tile_occupancy(const uint64_t* bv, int64_t n_cols, int64_t n_
     tile_occupancy_kernel<<<in_grid(n_cols * occ_ld), IN_THREADS, 0, as_stream(stream)>>>(bv, n_cols, n_words, ld, occ,
                                                                                          occ_ld);
     ETM_LAUNCHED("tile_occupancy");
+    return ETM_OK;
+}
+
+extern "C" int etm_item_codes(const int64_t* row_ptr, const int64_t* ids, int64_t nnz, int64_t n_rows, int64_t lo,
+                              int64_t span, uint32_t* bitmap, int64_t* word_rank, int32_t* codes, int32_t* status,
+                              void* stream) {
+    ETM_REQUIRE(nnz >= 0 && n_rows >= 0 && span >= 1 && span <= ETM_CODE_SPAN_MAX, ETM_EINVAL,
+                "etm_item_codes: span %lld outside [1, 2^26] or negative size", (long long)span);
+    ETM_REQUIRE(status != nullptr, ETM_EINVAL, "etm_item_codes: status is required");
+    cudaStream_t s = as_stream(stream);
+    const int64_t n_w = ceil_div<int64_t>(span, 32);
+    ETM_CUDA(cudaMemsetAsync(status, 0, 2 * sizeof(int32_t), s));
+    ETM_CUDA(cudaMemsetAsync(bitmap, 0, (size_t)n_w * 4, s));
+    int* st = reinterpret_cast<int*>(status);
+    if (nnz > 0) {
+        id_presence_kernel<<<(int)max64(1, min64((int64_t)max(1, sm_count()) * 8, ceil_div<int64_t>(nnz, IN_THREADS))),
+                             IN_THREADS, 0, s>>>(ids, nnz, lo, span, bitmap, st);
+        ETM_LAUNCHED("id_presence");
+    }
+    bitmap_rank_kernel<<<1, 1024, 0, s>>>(bitmap, n_w, word_rank);
+    ETM_LAUNCHED("bitmap_rank");
+    if (n_rows > 0) {
+        code_rows_kernel<<<in_grid(n_rows), IN_THREADS, 0, s>>>(row_ptr, ids, n_rows, lo, span, bitmap, word_rank,
+                                                               codes, st + 1);
+        ETM_LAUNCHED("code_rows");
+    }
+    return ETM_OK;
+}
+
+extern "C" int etm_code_histogram(const int32_t* codes, int64_t nnz, int64_t n_bins, int64_t* counts, void* stream) {
+    ETM_REQUIRE(nnz >= 0 && n_bins >= 0, ETM_EINVAL, "etm_code_histogram: negative size");
+    cudaStream_t s = as_stream(stream);
+    if (n_bins == 0) return ETM_OK;
+    ETM_CUDA(cudaMemsetAsync(counts, 0, (size_t)n_bins * 8, s));
+    if (nnz == 0) return ETM_OK;
+    auto* out = reinterpret_cast<unsigned long long*>(counts);
+    const int grid = (int)max64(1, min64((int64_t)max(1, sm_count()) * 4, ceil_div<int64_t>(nnz, IN_THREADS)));
+    if (n_bins <= HIST_SMEM_BINS) {
+        code_histogram_kernel<true><<<grid, IN_THREADS, (size_t)n_bins * 4, s>>>(codes, nnz, n_bins, out);
+    } else {
+        code_histogram_kernel<false><<<grid, IN_THREADS, 0, s>>>(codes, nnz, n_bins, out);
+    }
+    ETM_LAUNCHED("code_histogram");
+    return ETM_OK;
+}
+
+extern "C" int etm_bitmap_values(const uint32_t* bitmap, int64_t span, const int64_t* word_rank, int64_t lo,
+                                 int64_t* out, void* stream) {
+    ETM_REQUIRE(span >= 1 && span <= ETM_CODE_SPAN_MAX, ETM_EINVAL, "etm_bitmap_values: span out of range");
+    const int64_t n_w = ceil_div<int64_t>(span, 32);
+    bitmap_values_kernel<<<(int)min64((int64_t)max(1, sm_count()) * 8, ceil_div<int64_t>(n_w, IN_THREADS)), IN_THREADS,
+                           0, as_stream(stream)>>>(bitmap, n_w, word_rank, lo, out);
+    ETM_LAUNCHED("bitmap_values");
+    return ETM_OK;
+}
+
+extern "C" int etm_kept_lengths(const int64_t* row_ptr, const int32_t* codes, int64_t n_rows, const int32_t* lut,
+                                int64_t lut_size, int64_t* out_lengths, void* stream) {
+    ETM_REQUIRE(n_rows >= 0 && lut_size >= 0, ETM_EINVAL, "etm_kept_lengths: negative size");
+    if (n_rows == 0) return ETM_OK;
+    kept_lengths_kernel<<<in_grid(n_rows), IN_THREADS, 0, as_stream(stream)>>>(row_ptr, codes, n_rows, lut, lut_size,
+                                                                              out_lengths);
+    ETM_LAUNCHED("kept_lengths");
     return ETM_OK;
 }

@@ -1081,7 +1081,9 @@ class Engine:
              occupancy: bool = False) -> MineOutput:
         """Mine device bitvectors. ``rows`` = (row_ptr int64, cols int32, host row lengths) on the device,
         the transactions the bitvectors were built from, lets K=2 count row-wise when its rows are short
-        against the pair space (the reference's rule, gpu/row_split_chunks.py:124-142).
+        against the pair space (the reference's rule, gpu/row_split_chunks.py:124-142). A fourth element
+        (int32, -1 for none) makes the entries codes mapped to columns through it; the lengths then count
+        only the entries that map to a column.
 
         ``max_ram_gb`` / ``max_vram_gb``: after every level, the process's resident memory and the device
         memory allocated through torch (every engine buffer) are checked against them; over a limit the mine raises
@@ -1139,11 +1141,15 @@ class Engine:
         if occupancy:
             self._occ = self.tile_occupancy(fbv, ldp, n_words)
         if rows is not None:
-            rp, cl, lens = rows
+            rp, cl, lens = rows[:3]
             pair_work = float((lens.astype(np.float64) * (lens - 1) / 2).sum())
             lut = torch.full((max(1, n_cols),), -1, dtype=torch.int32, device=self.device)
             lut[torch.from_numpy(gen_cols.astype(np.int64)).to(self.device)] = torch.arange(
                 ng, dtype=torch.int32, device=self.device)
+            if len(rows) > 3:
+                # The entries hold codes and rows[3] their columns (-1 for none): compose code -> generator.
+                col_of = rows[3]
+                lut = torch.where(col_of >= 0, lut[col_of.clamp(min=0).long()], col_of).contiguous()
             self._rows_input = dict(rp=rp, cl=cl, nnz=int(cl.numel()), lut=lut, n_r=int(rp.numel()) - 1,
                                     pair_work=pair_work, ng=ng)
             r = pair_work / max(1.0, ng * (ng - 1) / 2 * n_words)

@@ -71,6 +71,8 @@ extern "C" {
 #define ETM_PROJ_SEG_WORDS 1024
 /* Words of one occupancy tile (2,048 transactions); 64 tiles per occupancy word. */
 #define ETM_OCC_TILE_WORDS 32
+/* Widest id span etm_item_codes codes through its presence bitmap (8 MB of bits). */
+#define ETM_CODE_SPAN_MAX (1LL << 26)
 
 int etm_version(void);
 /* Message of the last failing call on this thread (empty if none). */
@@ -136,6 +138,35 @@ int etm_permute_rows(const int64_t* row_ptr, const int32_t* cols, int64_t nnz, c
                      const int64_t* new_row_ptr, int32_t* new_cols, int32_t* status, void* stream);
 int etm_tile_occupancy(const uint64_t* bv, int64_t n_cols, int64_t n_words, int64_t ld, uint64_t* occ,
                        int64_t occ_ld, void* stream);
+
+/*
+ * Item coding of a transaction CSR without sorting (the device input layer's
+ * K=1 and id lookup, gpu/input_layer.py:396-466, with exact supports).
+ *   etm_item_codes     ids int64 [nnz] in rows row_ptr int64 [n_rows+1]; the
+ *                      ids lie in [lo, lo + span), span <= ETM_CODE_SPAN_MAX.
+ *                      bitmap uint32 [ceil(span/32)] gets bit id - lo of every
+ *                      id present; word_rank int64 [ceil(span/32) + 1] the set
+ *                      bits before each word (its last entry: the distinct
+ *                      ids); codes int32 [nnz] each entry's rank among the
+ *                      distinct ids (ascending id order). status int32 [2]
+ *                      (zeroed here): [0] = 1 when an id lies outside the span
+ *                      (its code is -1), [1] = 1 when a row's codes do not
+ *                      strictly ascend (unsorted, or an id repeated).
+ *   etm_code_histogram counts int64 [n_bins] = occurrences of each code (codes
+ *                      outside [0, n_bins) ignored); with canonical rows, the
+ *                      rows holding each id.
+ *   etm_bitmap_values  out int64 [distinct ids] = the ids present, ascending.
+ *   etm_kept_lengths   out_lengths int64 [n_rows] = each row's entries whose
+ *                      code maps to a column (lut int32 [lut_size], -1 none).
+ */
+int etm_item_codes(const int64_t* row_ptr, const int64_t* ids, int64_t nnz, int64_t n_rows, int64_t lo,
+                   int64_t span, uint32_t* bitmap, int64_t* word_rank, int32_t* codes, int32_t* status,
+                   void* stream);
+int etm_code_histogram(const int32_t* codes, int64_t nnz, int64_t n_bins, int64_t* counts, void* stream);
+int etm_bitmap_values(const uint32_t* bitmap, int64_t span, const int64_t* word_rank, int64_t lo, int64_t* out,
+                      void* stream);
+int etm_kept_lengths(const int64_t* row_ptr, const int32_t* codes, int64_t n_rows, const int32_t* lut,
+                     int64_t lut_size, int64_t* out_lengths, void* stream);
 
 /*
  * Deterministic Bernoulli bitvectors (workload generator; no reference

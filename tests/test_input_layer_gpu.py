@@ -197,3 +197,71 @@ def test_transactions_in_lex_order_match_input_order(pkg):
         got.append(pkg.result_pairs(df, 60_000))
     assert got[0] == got[1]
     assert max(len(s) for s, _ in got[0]) == 4
+
+
+def _canonical_csr(rng, n_rows: int, ids: np.ndarray, max_len: int):
+    lens = rng.integers(0, max_len + 1, n_rows)
+    lens[::31] = 0
+    rp = np.zeros(n_rows + 1, np.int64)
+    np.cumsum(lens, out=rp[1:])
+    flat = np.concatenate([np.sort(rng.choice(ids, size=int(k), replace=False)) for k in lens]) if lens.sum() \
+        else np.zeros(0, np.int64)
+    return rp, flat.astype(np.int64)
+
+
+@pytest.mark.parametrize("mc", [1, 40])
+def test_coded_input_matches_host(pkg, mc):
+    """The sort-free coding gives the columns, supports and rows of the host restatement."""
+    import torch
+
+    api = import_module(pkg.__name__ + ".api")
+    rng = np.random.default_rng(mc)
+    ids = np.unique(rng.integers(-5_000, 90_000, 300))
+    n_rows = 4_000
+    rp, flat = _canonical_csr(rng, n_rows, ids, 25)
+    rp_h, cols_h, items_h = api._frequent_csr(rp, flat, n_rows, mc)
+    got = api._coded_csr_device(rp, flat, n_rows, mc, torch.device("cuda"))
+    assert got is not None
+    assert np.array_equal(got.items, items_h)
+    assert np.array_equal(got.support, np.bincount(cols_h, minlength=len(items_h)))
+    assert np.array_equal(got.row_len, np.diff(rp_h))
+    cols = got.col_of[got.codes.long()].cpu().numpy()
+    assert np.array_equal(cols[cols >= 0], cols_h)
+    assert np.array_equal(got.row_ptr.cpu().numpy(), rp)
+    assert len(got.code_support) == len(np.unique(flat))
+
+
+def test_coded_input_declines_what_it_cannot_code(pkg):
+    """Rows with a repeated or unsorted id, ids beyond the bitmap's span and UInt64 ids take the sorting path."""
+    import torch
+
+    api = import_module(pkg.__name__ + ".api")
+    dev = torch.device("cuda")
+    rp = np.array([0, 3, 5], np.int64)
+    assert api._coded_csr_device(rp, np.array([1, 2, 2, 4, 7], np.int64), 2, 1, dev) is None  # repeated
+    assert api._coded_csr_device(rp, np.array([1, 3, 2, 4, 7], np.int64), 2, 1, dev) is None  # unsorted
+    assert api._coded_csr_device(rp, np.array([1, 2, 3, 4, 1 << 27], np.int64), 2, 1, dev) is None  # span
+    assert api._coded_csr_device(rp, np.array([1, 2, 3, 4, 7], np.uint64), 2, 1, dev) is None
+    got = api._coded_csr_device(rp, np.array([1, 2, 3, 4, 7], np.int64), 2, 1, dev)
+    assert got is not None and got.items.tolist() == [1, 2, 3, 4, 7]
+
+
+def test_item_codes_report_an_id_outside_the_span(pkg):
+    import torch
+
+    lib = pkg.load_library()
+    rp = torch.tensor([0, 2, 4], dtype=torch.int64, device="cuda")
+    ids = torch.tensor([3, 9, 4, 40], dtype=torch.int64, device="cuda")
+    span = 32
+    bitmap = torch.empty(1, dtype=torch.int32, device="cuda")
+    rank = torch.empty(2, dtype=torch.int64, device="cuda")
+    codes = torch.empty(4, dtype=torch.int32, device="cuda")
+    status = torch.empty(2, dtype=torch.int32, device="cuda")
+    st = lib.etm_item_codes(rp.data_ptr(), ids.data_ptr(), 4, 2, 0, span, bitmap.data_ptr(), rank.data_ptr(),
+                            codes.data_ptr(), status.data_ptr(), _stream())
+    assert st == 0, lib.etm_last_error()
+    assert status.cpu().tolist() == [1, 1]  # 40 lies outside [0, 32); its row is then not canonical either
+    assert codes.cpu().tolist() == [0, 2, 1, -1]
+    assert rank.cpu().tolist() == [0, 3]
+    assert lib.etm_item_codes(rp.data_ptr(), ids.data_ptr(), 4, 2, 0, (1 << 26) + 1, bitmap.data_ptr(),
+                              rank.data_ptr(), codes.data_ptr(), status.data_ptr(), _stream()) == 1
