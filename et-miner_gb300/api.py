@@ -323,13 +323,13 @@ def _coded_csr_device(indptr: np.ndarray, flat: np.ndarray, n_rows: int, mc: int
     nnz = len(flat)
     if nnz == 0 or n_rows == 0 or flat.dtype == np.uint64 or not np.issubdtype(flat.dtype, np.integer):
         return None
-    lib = load_library()
-    stream = torch.cuda.current_stream(device).cuda_stream
     vals = torch.from_numpy(np.ascontiguousarray(flat).astype(np.int64, copy=False)).to(device)
     lo_hi = torch.stack(torch.aminmax(vals)).cpu().numpy()
     lo, span = int(lo_hi[0]), int(lo_hi[1]) - int(lo_hi[0]) + 1
     if span > CODE_SPAN_MAX:
         return None
+    lib = load_library()
+    stream = torch.cuda.current_stream(device).cuda_stream
     n_w = -(-span // 32)
     row_ptr = torch.from_numpy(np.ascontiguousarray(indptr, dtype=np.int64)).to(device)
     bitmap = torch.empty(n_w, dtype=torch.int32, device=device)

@@ -34,6 +34,18 @@ def test_device_frequent_csr_matches_host(pkg, wide, mc):
     assert np.array_equal(support, np.bincount(cols_h, minlength=len(items_h)))
 
 
+def test_sort_free_coding_declines_before_any_kernel(pkg):
+    """The sort-free coding hands UInt64 ids, non-integer values, empty inputs and id spans past 2^26 to the
+    sorting path; all of these are decided before the library is called (here, on the CPU)."""
+    api = import_module(pkg.__name__ + ".api")
+    rp = np.array([0, 2, 3], np.int64)
+    assert api._coded_csr_device(rp, np.array([1, 2, 3], np.uint64), 2, 1, "cpu") is None
+    assert api._coded_csr_device(rp, np.array([1.0, 2.0, 3.0]), 2, 1, "cpu") is None
+    assert api._coded_csr_device(np.zeros(3, np.int64), np.zeros(0, np.int64), 2, 1, "cpu") is None
+    assert api._coded_csr_device(rp, np.array([-5, 2, (1 << 26) - 5], np.int64), 2, 1, "cpu") is None
+    assert api.CODE_SPAN_MAX == 1 << 26
+
+
 @pytest.mark.parametrize("kw,exc,match", [
     (dict(min_support=1.5), ValueError, r"\[0.0, 1.0\]"),
     (dict(min_support="0.1"), TypeError, "numeric"),
