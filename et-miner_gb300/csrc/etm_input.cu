@@ -1,6 +1,8 @@
-// The input layer's row order and tile occupancy: sort keys that gather the rows sharing their most
-// frequent columns (the lex row order), the transaction CSR permuted into that order, and per column one
-// bit per 32-word tile holding a row of it, which lets the prefix and per-candidate kernels skip tiles.
+// The device input layer: the item coding of a transaction CSR without sorting (a presence bitmap over the
+// id span ranks every id; rows are checked to be canonical; a histogram of the ranks gives the supports),
+// the lex row order (sort keys that gather the rows sharing their most frequent columns, and the CSR
+// permuted into that order), and the tile occupancy (per column one bit per 32-word tile holding a row of
+// it, which lets the prefix and per-candidate kernels skip tiles).
 //
 // HBM-bound integer work: warps over rows / occupancy words, grids a multiple of the SM count.
 #include "etm_common.cuh"
