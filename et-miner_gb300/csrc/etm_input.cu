@@ -74,8 +74,10 @@ __global__ void __launch_bounds__(IN_THREADS) permute_rows_kernel(const int64_t*
 }
 
 // occ[c][ow], bit b: tile t = 64 ow + b of column c (words [32 t, 32 t + 32) below n_words) holds a set bit
-// (the occupancy of gpu/kernels/occupancy.py:37-58). One warp per occupancy word, 32 steps of 16-byte loads:
-// lanes 0-15 read tile 2 i of step i, lanes 16-31 tile 2 i + 1.
+// (the occupancy of gpu/kernels/occupancy.py:37-58). One warp per occupancy word, 32 steps of two words per
+// lane: lanes 0-15 read tile 2 i of step i, lanes 16-31 tile 2 i + 1; one 16-byte load per lane when every
+// column starts 16-byte aligned (VEC), else two 8-byte loads.
+template <bool VEC>
 __global__ void __launch_bounds__(IN_THREADS) tile_occupancy_kernel(const uint64_t* __restrict__ bv, int64_t n_cols,
                                                                     int64_t n_words, int64_t ld,
                                                                     uint64_t* __restrict__ occ, int64_t occ_ld) {
@@ -92,8 +94,12 @@ __global__ void __launch_bounds__(IN_THREADS) tile_occupancy_kernel(const uint64
             const int64_t w = w0 + 64 * i;
             uint64_t x = 0;
             if (w + 1 < n_words) {
-                const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(col + w));
-                x = v.x | v.y;
+                if (VEC) {
+                    const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(col + w));
+                    x = v.x | v.y;
+                } else {
+                    x = __ldg(col + w) | __ldg(col + w + 1);
+                }
             } else if (w < n_words) {
                 x = __ldg(col + w);
             }
@@ -270,14 +276,16 @@ extern "C" int etm_permute_rows(const int64_t* row_ptr, const int32_t* cols, int
 extern "C" int etm_tile_occupancy(const uint64_t* bv, int64_t n_cols, int64_t n_words, int64_t ld, uint64_t* occ,
                                   int64_t occ_ld, void* stream) {
     ETM_REQUIRE(n_cols >= 0 && n_words >= 0 && ld >= n_words, ETM_EINVAL, "etm_tile_occupancy: bad sizes");
-    ETM_REQUIRE(ld % 2 == 0 && (reinterpret_cast<uintptr_t>(bv) & 15) == 0, ETM_EINVAL,
-                "etm_tile_occupancy: bv must be 16-byte aligned with an even ld");
+    ETM_REQUIRE((reinterpret_cast<uintptr_t>(bv) & 7) == 0, ETM_EINVAL, "etm_tile_occupancy: bv must be 8-byte aligned");
     const int64_t tiles = ceil_div<int64_t>(n_words, ETM_OCC_TILE_WORDS);
     ETM_REQUIRE(occ_ld >= ceil_div<int64_t>(tiles, 64) && occ_ld >= 1, ETM_EINVAL,
                 "etm_tile_occupancy: occ_ld %lld < ceil(tiles / 64)", (long long)occ_ld);
     if (n_cols == 0) return ETM_OK;
-    tile_occupancy_kernel<<<in_grid(n_cols * occ_ld), IN_THREADS, 0, as_stream(stream)>>>(bv, n_cols, n_words, ld, occ,
-                                                                                         occ_ld);
+    const int grid = in_grid(n_cols * occ_ld);
+    if (ld % 2 == 0 && (reinterpret_cast<uintptr_t>(bv) & 15) == 0)
+        tile_occupancy_kernel<true><<<grid, IN_THREADS, 0, as_stream(stream)>>>(bv, n_cols, n_words, ld, occ, occ_ld);
+    else
+        tile_occupancy_kernel<false><<<grid, IN_THREADS, 0, as_stream(stream)>>>(bv, n_cols, n_words, ld, occ, occ_ld);
     ETM_LAUNCHED("tile_occupancy");
     return ETM_OK;
 }

@@ -130,7 +130,8 @@ int etm_gather_cols(const uint64_t* bv, int64_t ld, const int32_t* cols, int32_t
  *                      words (gpu/kernels/occupancy.py:37-58): bit b of
  *                      occ[c * occ_ld + w] is set when tile 64 w + b (words
  *                      below n_words) holds a set bit. occ_ld >= ceil(ceil(
- *                      n_words / 32) / 64); bv 16-byte aligned, ld even.
+ *                      n_words / 32) / 64); any ld >= n_words (16-byte loads
+ *                      when bv is 16-byte aligned and ld even).
  */
 int etm_row_order_keys(const int64_t* row_ptr, const int32_t* cols, int64_t n_rows, const int32_t* rank_of_col,
                        int64_t n_cols, int64_t* key_hi, int64_t* key_lo, void* stream);

@@ -101,13 +101,18 @@ def test_permute_rows_refuses_a_bad_order(pkg):
 
 
 @pytest.mark.parametrize("n_words", [1, 31, 32, 33, 2_047, 2_048, 2_049, 5_000])
-def test_tile_occupancy_matches_host(pkg, n_words):
+@pytest.mark.parametrize("odd_ld", [False, True])
+def test_tile_occupancy_matches_host(pkg, n_words, odd_ld):
+    """Padded columns (16-byte loads) and the reference's own layout, ld = the words per column (8-byte loads
+    where a column starts off a 16-byte boundary)."""
     import torch
 
     lib = pkg.load_library()
     rng = np.random.default_rng(n_words)
     n_cols = 7
     ld = n_words + (n_words % 2) + 2
+    if odd_ld:
+        ld = n_words + 1 - (n_words % 2)
     bv = np.zeros((n_cols, ld), np.uint64)
     for c in range(n_cols):
         # A few words set per column, some columns empty, garbage past n_words that must be ignored.
