@@ -50,15 +50,16 @@ def _random_csr(rng, n_rows: int, n_cols: int, max_len: int):
     return rp, cols
 
 
-@pytest.mark.parametrize("n_cols", [40, 200])
-def test_row_order_keys_and_permutation(pkg, n_cols):
+@pytest.mark.parametrize("n_cols,max_len", [(40, 30), (200, 30), (300, 150)])
+def test_row_order_keys_and_permutation(pkg, n_cols, max_len):
+    """Rows of up to 150 entries take several warp-wide steps per row."""
     import torch
 
     api = import_module(pkg.__name__ + ".api")
     lib = pkg.load_library()
     rng = np.random.default_rng(n_cols)
     n_rows = 3_001
-    rp, cols = _random_csr(rng, n_rows, n_cols, 30)
+    rp, cols = _random_csr(rng, n_rows, n_cols, max_len)
     support = np.bincount(cols, minlength=n_cols)
     rank = np.empty(n_cols, np.int32)
     rank[np.argsort(-support, kind="stable")] = np.arange(n_cols, dtype=np.int32)
@@ -214,16 +215,17 @@ def _canonical_csr(rng, n_rows: int, ids: np.ndarray, max_len: int):
     return rp, flat.astype(np.int64)
 
 
-@pytest.mark.parametrize("mc", [1, 40])
-def test_coded_input_matches_host(pkg, mc):
-    """The sort-free coding gives the columns, supports and rows of the host restatement."""
+@pytest.mark.parametrize("mc,max_len", [(1, 25), (40, 25), (40, 200)])
+def test_coded_input_matches_host(pkg, mc, max_len):
+    """The sort-free coding gives the columns, supports and rows of the host restatement (rows of up to 200
+    ids take several warp-wide steps, and the canonical check carries across them)."""
     import torch
 
     api = import_module(pkg.__name__ + ".api")
-    rng = np.random.default_rng(mc)
-    ids = np.unique(rng.integers(-5_000, 90_000, 300))
+    rng = np.random.default_rng(mc + max_len)
+    ids = np.unique(rng.integers(-5_000, 90_000, 300 if max_len < 100 else 600))
     n_rows = 4_000
-    rp, flat = _canonical_csr(rng, n_rows, ids, 25)
+    rp, flat = _canonical_csr(rng, n_rows, ids, max_len)
     rp_h, cols_h, items_h = api._frequent_csr(rp, flat, n_rows, mc)
     got = api._coded_csr_device(rp, flat, n_rows, mc, torch.device("cuda"))
     assert got is not None
@@ -244,6 +246,11 @@ def test_coded_input_declines_what_it_cannot_code(pkg):
     dev = torch.device("cuda")
     rp = np.array([0, 3, 5], np.int64)
     assert api._coded_csr_device(rp, np.array([1, 2, 2, 4, 7], np.int64), 2, 1, dev) is None  # repeated
+    # A repeat across the boundary of two warp-wide steps of one row (entries 31 and 32).
+    long_row = np.concatenate([np.arange(32), [31], np.arange(40, 50)]).astype(np.int64)
+    assert api._coded_csr_device(np.array([0, len(long_row)], np.int64), long_row, 1, 1, dev) is None
+    ok_row = np.concatenate([np.arange(32), np.arange(40, 50)]).astype(np.int64)
+    assert api._coded_csr_device(np.array([0, len(ok_row)], np.int64), ok_row, 1, 1, dev) is not None
     assert api._coded_csr_device(rp, np.array([1, 3, 2, 4, 7], np.int64), 2, 1, dev) is None  # unsorted
     assert api._coded_csr_device(rp, np.array([1, 2, 3, 4, 1 << 27], np.int64), 2, 1, dev) is None  # span
     assert api._coded_csr_device(rp, np.array([1, 2, 3, 4, 7], np.uint64), 2, 1, dev) is None
