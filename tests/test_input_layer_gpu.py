@@ -238,6 +238,24 @@ def test_coded_input_matches_host(pkg, mc, max_len):
     assert len(got.code_support) == len(np.unique(flat))
 
 
+def test_coded_input_with_more_ids_than_shared_counters(pkg):
+    """More distinct ids than the histogram's block-private counters hold: the global-atomic form."""
+    import torch
+
+    api = import_module(pkg.__name__ + ".api")
+    rng = np.random.default_rng(5)
+    ids = np.unique(rng.integers(0, 400_000, 30_000))
+    n_rows = 20_000
+    rp, flat = _canonical_csr(rng, n_rows, ids, 40)
+    mc = 3
+    rp_h, cols_h, items_h = api._frequent_csr(rp, flat, n_rows, mc)
+    got = api._coded_csr_device(rp, flat, n_rows, mc, torch.device("cuda"))
+    assert got is not None and len(got.code_support) > 12_288
+    assert np.array_equal(got.items, items_h)
+    assert np.array_equal(got.support, np.bincount(cols_h, minlength=len(items_h)))
+    assert np.array_equal(got.row_len, np.diff(rp_h))
+
+
 def test_coded_input_declines_what_it_cannot_code(pkg):
     """Rows with a repeated or unsorted id, ids beyond the bitmap's span and UInt64 ids take the sorting path."""
     import torch
